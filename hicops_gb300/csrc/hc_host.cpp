@@ -1,0 +1,211 @@
+// Host-side preparation for the DSLIM path: ion-key tables, the lgfact
+// table, database-entry enumeration (base peptides + variable-mod variants)
+// and the division constants used by the query kernel.
+//
+// Compiled with -ffp-contract=off: the tables are derived with the same
+// double arithmetic the reference uses, and must round the same way on
+// x86-64 and aarch64.
+#include <cmath>
+#include <cstring>
+
+#include "hc_internal.h"
+
+namespace hc {
+
+namespace {
+
+// Residue masses and the static carbamidomethyl-C mod (utils.cpp:41-98),
+// single precision as in the reference.
+constexpr float kNaa = -20000.0f;
+const float kAAMass[26] = {
+    71.03712f, kNaa, 103.00919f, 115.030f, 129.0426f, 147.068f, 57.02146f, 137.060f,
+    113.084f,  kNaa, 128.094f,   113.084f, 131.0405f, 114.043f, kNaa,      97.0527f,
+    128.05858f, 156.1012f, 87.032f, 101.0476f, kNaa, 99.06841f, 186.0793f, kNaa,
+    163.0633f, kNaa};
+const float kStatMods[26] = {0, 0, 57.021464f, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                             0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+constexpr float kH2O = 18.015f;
+constexpr double kProton = 1.00727647;
+
+// GETAA(x, z) (utils.cpp:101): float residue + float static mod, then the
+// proton mass times z added in double.
+inline double getaa(int a, double z)
+{
+    float s = kAAMass[a] + kStatMods[a];
+    return (double)s + kProton * z;
+}
+
+float pep_mass(const uint8_t *seq, uint32_t L)
+{
+    // UTILS_CalculatePepMass (utils.cpp:290-303): two float additions per residue
+    float m = kH2O;
+    for (uint32_t l = 0; l < L; l++)
+    {
+        m += kAAMass[seq[l] - 'A'];
+        m += kStatMods[seq[l] - 'A'];
+    }
+    return m;
+}
+
+float mod_mass(const hc_params &p, const uint8_t *seq, uint32_t L, uint32_t modnum)
+{
+    // UTILS_CalculateModMass (utils.cpp:337-362): its loop advances `start`
+    // by a shift of 4 but then shifts the masked value right by `start`
+    // itself; the hardware takes that count mod 32, the result is 0, so
+    // only the first mod's scaled mass (as float / scale) is added.
+    float m = pep_mass(seq, L);
+    uint32_t first = modnum & 0xF;
+    if (first != 0)
+        m += (float)p.mod_mass[first - 1] / (float)p.scale;
+    return m;
+}
+
+struct VariantGen
+{
+    const hc_params *p;
+    int cond_of[26];
+    const uint8_t *seq;
+    uint32_t L, seqid;
+    hc_entry *out;
+    int64_t n, cap;
+
+    // Depth-first enumeration of MODS_ModList (mods.cpp:333-384): at each
+    // position first the branch that modifies it, then the one that does
+    // not; an entry is emitted on entering a position right after a new mod.
+    void walk(int *conds, int total, uint64_t sites, uint32_t modnum, int letter, bool novel,
+              int seen)
+    {
+        if (novel && letter != 0)
+        {
+            if (n < cap && out)
+            {
+                hc_entry &e = out[n];
+                e.seqid = seqid;
+                e.sites = sites;
+                e.modnum = modnum;
+                e.pad = 0;
+                e.mass = mod_mass(*p, seq, L, modnum);
+            }
+            n++;
+        }
+        if (total == 0 || letter >= (int)L)
+            return;
+        int c = cond_of[seq[letter] - 'A'];
+        if (c != -1 && conds[c] > 0)
+        {
+            conds[c] -= 1;
+            walk(conds, total - 1, sites | (1ull << letter),
+                 modnum + (uint32_t)((1u << (4 * seen)) * (uint32_t)(1 + c)), letter + 1, true,
+                 seen + 1);
+            conds[c] += 1;
+        }
+        walk(conds, total, sites, modnum, letter + 1, false, seen);
+    }
+};
+
+}  // namespace
+
+void make_ion_tables(const hc_params &p, IonTables *t)
+{
+    std::memset(t, 0, sizeof(*t));
+    const double scale = p.scale;
+    for (int a = 0; a < 26; a++)
+    {
+        for (uint32_t z = 0; z < p.maxz && z < (uint32_t)kMaxZ; z++)
+        {
+            // UTILS_GenerateSpectrum, utils.cpp:257-270
+            t->bf[a][z] = (uint32_t)((getaa(a, z + 1) * scale) / (z + 1));
+            t->yf[a][z] = (uint32_t)(((getaa(a, z + 1) + kH2O) * scale) / (z + 1));
+            t->inc[a][z] = (uint32_t)((getaa(a, 0) * scale) / (z + 1));
+            // UTILS_GenerateModSpectrum, utils.cpp:441-454 (division comes later)
+            t->bfm[a][z] = (uint32_t)(getaa(a, z + 1) * scale);
+            t->yfm[a][z] = (uint32_t)((getaa(a, z + 1) + kH2O) * scale);
+        }
+        t->incm[a] = (uint32_t)(getaa(a, 0) * scale);
+    }
+    for (uint32_t m = 0; m < p.nmods && m < 16; m++)
+        t->mod_mass[m] = p.mod_mass[m];
+    t->maxz = p.maxz;
+    t->scale = p.scale;
+    t->min_mass = p.min_mass;
+    t->max_mass = p.max_mass;
+}
+
+void make_query_const(QueryConst *q)
+{
+    // hcp::utils::lgfact (utils.h:115-131): val[0] = val[1] = log10(1),
+    // val[i] = log10(i) + val[i-1]. Entries past 80 exist only so that the
+    // device never reads out of bounds; results using them are flagged.
+    q->lgfact[0] = q->lgfact[1] = std::log10(1.0);
+    for (int i = 2; i < kLgTable; i++)
+        q->lgfact[i] = std::log10((double)i) + q->lgfact[i - 1];
+    for (int i = 0; i < kLgTable; i++)
+        q->lgfact_f[i] = (float)q->lgfact[i];
+}
+
+int64_t make_entries(const hc_params &p, uint32_t L, const uint8_t *seqs, uint32_t npep,
+                     hc_entry *out, int64_t cap)
+{
+    // LBE_GeneratePeps (lbe_internal.cpp:204-229): one entry per peptide, in
+    // file order; then the variants of MODS_GenerateMods (mods.cpp:448-496),
+    // peptide by peptide.
+    VariantGen g{};
+    g.p = &p;
+    g.L = L;
+    g.out = out;
+    g.cap = cap;
+    for (int i = 0; i < 26; i++) g.cond_of[i] = -1;
+    for (uint32_t m = 0; m < p.nmods && m < HC_MAX_MODS; m++)
+        for (int j = 0; j < 4 && p.mod_res[m][j]; j++)
+        {
+            int c = p.mod_res[m][j] - 'A';
+            if (c >= 0 && c < 26) g.cond_of[c] = (int)m;
+        }
+    for (uint32_t i = 0; i < npep; i++)
+    {
+        if (out && g.n < cap)
+        {
+            hc_entry &e = out[g.n];
+            e.mass = pep_mass(seqs + (size_t)i * L, L);
+            e.seqid = i;
+            e.sites = 0;
+            e.modnum = 0;
+            e.pad = 0;
+        }
+        g.n++;
+    }
+    if (p.vmods_per_pep > 0 && p.nmods > 0)
+    {
+        int conds[HC_MAX_MODS] = {0};
+        for (uint32_t m = 0; m < p.nmods && m < HC_MAX_MODS; m++) conds[m] = (int)p.mod_per_pep[m];
+        for (uint32_t i = 0; i < npep; i++)
+        {
+            g.seq = seqs + (size_t)i * L;
+            g.seqid = i;
+            g.walk(conds, (int)p.vmods_per_pep, 0, 0, 0, false, 0);
+        }
+    }
+    return g.n;
+}
+
+void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh)
+{
+    // Granlund & Montgomery, "Division by Invariant Integers using
+    // Multiplication" (PLDI 1994), Thm 4.2 with N = 31-bit dividends:
+    // l = ceil(log2 d), m = ceil(2^(31+l) / d) < 2^32, and
+    // floor(x/d) = floor(m*x / 2^(31+l)) = umulhi(x, m) >> (l-1).
+    uint32_t l = 0;
+    while ((1ull << l) < d) l++;
+    if (l == 0)
+    {   // d == 1: umulhi(x, 2^31) = x >> 1, so use l = 1 and m = 2^32 - 1? keep exact:
+        *magic = 0xFFFFFFFFu;  // not used: speclen >= 2 always
+        *sh = 0;
+        return;
+    }
+    const unsigned __int128 num = (unsigned __int128)1 << (31 + l);
+    const uint64_t m = (uint64_t)((num + d - 1) / d);
+    *magic = (uint32_t)m;
+    *sh = l - 1;
+}
+
+}  // namespace hc

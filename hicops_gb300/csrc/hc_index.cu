@@ -1,0 +1,472 @@
+// Device construction of the SLM index of one peptide length
+// (DSLIM_Construct, source/core/dslim.cpp:46-138):
+//   1. entries sorted by mass on the device (stable LSD radix sort; the
+//      reference uses std::sort, lbe_internal.cpp:184-187),
+//   2. ion keys of every entry from integer tables (UTILS_GenerateSpectrum /
+//      UTILS_GenerateModSpectrum, utils.cpp:231-505, with the legality rules
+//      of DSLIM_ConstructChunk, dslim.cpp:296-323),
+//   3. postings iA = ion ids stably sorted by key (the reference's key/value
+//      quicksort + per-bucket sort, dslim.cpp:361-388 and 452-482, leave ids
+//      ascending inside every bucket: a stable sort gives exactly that),
+//   4. bucket offsets bA from the sorted keys (the exclusive scan of
+//      dslim.cpp:97-125).
+#include <cstdio>
+
+#include "hc_internal.h"
+
+namespace hc {
+namespace {
+
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 16;
+constexpr int kRsTile = kRsThreads * kRsItems;  // 4096 items per CTA
+constexpr int kRadix = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---- stable LSD radix sort, 8-bit digits ----------------------------------
+
+__global__ void k_rs_upsweep(const uint32_t *__restrict__ keys, size_t n, int shift,
+                             uint32_t *__restrict__ tile_hist, uint32_t ntiles)
+{
+    __shared__ uint32_t h[kRadix];
+    for (int i = threadIdx.x; i < kRadix; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kRsTile;
+#pragma unroll 4
+    for (int i = 0; i < kRsItems; i++)
+    {
+        size_t idx = base + (size_t)i * kRsThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 0xFF], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+        tile_hist[(size_t)d * ntiles + blockIdx.x] = h[d];
+}
+
+// Stable ranking: warp w owns items [w*512, w*512+512) of the tile in order;
+// inside a round of 32 items, lanes with equal digits are ranked by lane id
+// (match.any + lanemask_lt), rounds advance a per-warp digit counter, and the
+// warps' counters are scanned per digit.
+__global__ void k_rs_downsweep(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+                               uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
+                               size_t n, int shift, const uint32_t *__restrict__ tile_off,
+                               uint32_t ntiles, int write_keys)
+{
+    __shared__ uint32_t whist[kRsWarps][kRadix];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kRsWarps * kRadix; i += blockDim.x) (&whist[0][0])[i] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kRsTile + (size_t)warp * (kRsItems * 32);
+    uint32_t k[kRsItems], v[kRsItems], rank[kRsItems];
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++)
+    {
+        const size_t idx = base + (size_t)r * 32 + lane;
+        const bool ok = idx < n;
+        k[r] = ok ? keys_in[idx] : 0u;
+        v[r] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
+        const uint32_t d = ok ? ((k[r] >> shift) & 0xFF) : 0x100u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t before = (d < kRadix) ? whist[warp][d] : 0u;
+        rank[r] = before + __popc(peers & lt);
+        __syncwarp();
+        if (d < kRadix && (peers >> lane) == 1u)  // highest lane of the group
+            whist[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+    {
+        uint32_t run = tile_off[(size_t)d * ntiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kRsWarps; w++)
+        {
+            uint32_t c = whist[w][d];
+            whist[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++)
+    {
+        const size_t idx = base + (size_t)r * 32 + lane;
+        if (idx < n)
+        {
+            const uint32_t d = (k[r] >> shift) & 0xFF;
+            const uint32_t dst = whist[warp][d] + rank[r];
+            if (write_keys) keys_out[dst] = k[r];
+            vals_out[dst] = v[r];
+        }
+    }
+}
+
+// ---- exclusive scan of u32 (in place), recursive over block sums ----------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void k_scan_tiles(uint32_t *__restrict__ a, size_t n, uint32_t *__restrict__ sums)
+{
+    __shared__ uint32_t wsum[32];
+    const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t x[kScanItems], t = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++)
+    {
+        x[i] = (base + i < n) ? a[base + i] : 0u;
+        uint32_t c = x[i];
+        x[i] = t;
+        t += c;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+        if (lane >= o) s += y;
+    }
+    if (lane == 31) wsum[warp] = s;
+    __syncthreads();
+    if (warp == 0)
+    {
+        uint32_t w = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += y;
+        }
+        wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t excl = s - t + (warp ? wsum[warp - 1] : 0u);
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++)
+        if (base + i < n) a[base + i] = x[i] + excl;
+    if (threadIdx.x == kScanThreads - 1 && sums) sums[blockIdx.x] = excl + t;
+}
+
+__global__ void k_scan_add(uint32_t *__restrict__ a, size_t n, const uint32_t *__restrict__ sums)
+{
+    const uint32_t off = sums[blockIdx.x];
+    const size_t base = (size_t)blockIdx.x * kScanTile;
+    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x)
+        if (base + i < n) a[base + i] += off;
+}
+
+cudaError_t scan_exclusive(uint32_t *a, size_t n, uint32_t *tmp, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    const size_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 1)
+    {
+        k_scan_tiles<<<1, kScanThreads, 0, st>>>(a, n, nullptr);
+        return cudaGetLastError();
+    }
+    k_scan_tiles<<<(unsigned)nb, kScanThreads, 0, st>>>(a, n, tmp);
+    cudaError_t e = scan_exclusive(tmp, nb, tmp + nb, st);
+    if (e != cudaSuccess) return e;
+    k_scan_add<<<(unsigned)nb, 256, 0, st>>>(a, n, tmp);
+    return cudaGetLastError();
+}
+
+size_t scan_tmp_words(size_t n)
+{
+    size_t t = 0;
+    while (n > (size_t)kScanTile)
+    {
+        n = (n + kScanTile - 1) / kScanTile;
+        t += n;
+    }
+    return t + 16;
+}
+
+// Sorts (keys, vals) by the low `bits` bits of the keys, stably. Ping-pongs
+// between the given buffers; returns which buffer holds the result (0 or 1).
+// vals0 may be null: the values are then the input positions.
+cudaError_t radix_sort(uint32_t *keys0, uint32_t *keys1, uint32_t *vals0, uint32_t *vals1, size_t n,
+                       int bits, uint32_t *hist, uint32_t *scan_tmp, cudaStream_t st, int *which,
+                       int *launches, bool keys_out)
+{
+    const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
+    int cur = 0;
+    const uint32_t *vin = vals0;
+    for (int shift = 0; shift < bits; shift += 8)
+    {
+        uint32_t *kin = cur ? keys1 : keys0, *kout = cur ? keys0 : keys1;
+        uint32_t *vout = cur ? vals0 : vals1;
+        if (n)
+        {
+            k_rs_upsweep<<<ntiles, kRsThreads, 0, st>>>(kin, n, shift, hist, ntiles);
+            cudaError_t e = scan_exclusive(hist, (size_t)ntiles * kRadix, scan_tmp, st);
+            if (e != cudaSuccess) return e;
+            const int last = shift + 8 >= bits;
+            k_rs_downsweep<<<ntiles, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, hist,
+                                                          ntiles, (last && !keys_out) ? 0 : 1);
+            *launches += 3;
+        }
+        vin = vout;
+        cur ^= 1;
+    }
+    *which = cur;
+    return cudaGetLastError();
+}
+
+// ---- entries ---------------------------------------------------------------
+
+__global__ void k_mass_keys(const float *__restrict__ mass, uint32_t n, uint32_t *__restrict__ keys)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        uint32_t b = __float_as_uint(mass[i]);
+        keys[i] = (b & 0x80000000u) ? ~b : (b | 0x80000000u);  // total order of floats
+    }
+}
+
+__global__ void k_gather_entries(const uint32_t *__restrict__ perm, uint32_t n, const float *mass_in,
+                                 const uint32_t *seqid_in, const uint64_t *sites_in,
+                                 const uint32_t *modnum_in, float *mass, uint32_t *seqid,
+                                 uint64_t *sites, uint32_t *modnum)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const uint32_t j = perm[i];
+        mass[i] = mass_in[j];
+        seqid[i] = seqid_in[j];
+        sites[i] = sites_in[j];
+        modnum[i] = modnum_in[j];
+    }
+}
+
+// ---- ion keys ----------------------------------------------------------------
+// One thread per (entry, series, charge): writes the L-1 keys of one b or y
+// series. Layout per entry: [b z=1][b z=2]..[y z=1][y z=2].., each L-1 long
+// (utils.cpp:251-252).
+__global__ void k_ion_keys(const IonTables *__restrict__ gt, uint32_t L, uint32_t n,
+                           const float *__restrict__ mass, const uint32_t *__restrict__ seqid,
+                           const uint64_t *__restrict__ sites, const uint32_t *__restrict__ modnum,
+                           const uint8_t *__restrict__ seqs, uint32_t *__restrict__ keys,
+                           uint32_t *__restrict__ nuninit)
+{
+    __shared__ IonTables t;
+    for (int i = threadIdx.x; i < (int)(sizeof(IonTables) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t *>(&t)[i] = reinterpret_cast<const uint32_t *>(gt)[i];
+    __syncthreads();
+    const uint32_t maxz = t.maxz, nser = 2 * maxz;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)n * nser) return;
+    const uint32_t k = (uint32_t)(gid / nser), s = (uint32_t)(gid % nser);
+    const bool isY = s >= maxz;
+    const uint32_t z = isY ? s - maxz : s;
+    const uint32_t Lm1 = L - 1, speclen = nser * Lm1;
+    uint32_t *out = keys + (size_t)k * speclen + (isY ? maxz * Lm1 : 0) + z * Lm1;
+    const uint8_t *seq = seqs + (size_t)seqid[k] * L;
+    const double m = mass[k];
+    const double minm = t.min_mass, maxm = t.max_mass;
+    const uint32_t top = t.max_mass * t.scale;
+    const uint32_t mn = modnum[k];
+    bool legal = (m >= minm && m <= maxm);
+    if (mn != 0 && legal && !(m > minm && m < maxm))
+    {   // mass exactly on a bound: the reference reads an uninitialised spectrum
+        if (s == 0) atomicAdd(nuninit, 1u);
+        legal = false;
+    }
+    if (!legal)
+    {
+        for (uint32_t l = 0; l < Lm1; l++) out[l] = 0;
+        return;
+    }
+    if (mn == 0)
+    {
+        uint32_t v = isY ? t.yf[seq[L - 1] - 'A'][z] : t.bf[seq[0] - 'A'][z];
+        out[0] = v >= top ? top - 1 : v;
+        for (uint32_t l = 1; l < Lm1; l++)
+        {
+            const uint8_t a = isY ? seq[L - 1 - l] : seq[l];
+            v += t.inc[a - 'A'][z];
+            out[l] = v >= top ? top - 1 : v;
+        }
+        return;
+    }
+    // variable mods (utils.cpp:407-500): undivided running sums, plus the
+    // masses of the first `counter` mods (b) or last `counter` mods (y),
+    // then integer division by the charge
+    uint32_t mods[16];
+    int seen = 0;
+    {
+        uint32_t bm = mn;
+        for (int i = 0; i < 8; i++)
+        {
+            int q = (int)(bm & 0xF) - 1;
+            bm >>= 4;
+            if (q != -1) mods[seen++] = t.mod_mass[q & 15];
+        }
+    }
+    const uint64_t st = sites[k];
+    uint32_t v = isY ? t.yfm[seq[L - 1] - 'A'][z] : t.bfm[seq[0] - 'A'][z];
+    uint32_t madd = 0;
+    int cnt = 0;
+    for (uint32_t l = 0; l < Lm1; l++)
+    {
+        const uint32_t pos = isY ? (L - 1 - l) : l;
+        if (l > 0) v += t.incm[seq[pos] - 'A'];
+        if (((st >> pos) & 1ull) && cnt < seen)
+        {
+            madd += isY ? mods[seen - 1 - cnt] : mods[cnt];
+            cnt++;
+        }
+        uint32_t o = (v + madd) / (z + 1);
+        out[l] = o >= top ? top - 1 : o;
+    }
+}
+
+__global__ void k_bucket_bounds(const uint32_t *__restrict__ skeys, size_t M, uint32_t nb,
+                                uint32_t *__restrict__ bA)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > M) return;
+    // bA[b] = first position whose key >= b, for b in (key[i-1], key[i]]
+    const int64_t prev = (i == 0) ? -1 : (int64_t)skeys[i - 1];
+    const int64_t cur = (i == M) ? (int64_t)nb : (int64_t)skeys[i];
+    for (int64_t b = prev + 1; b <= cur; b++) bA[b] = (uint32_t)i;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n)
+{
+    return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1));
+}
+
+}  // namespace
+
+int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass)
+{
+    cudaStream_t st = ctx->stream;
+    const uint32_t n = lh.n, L = lh.L;
+    const uint32_t speclen = 2 * ctx->p.maxz * (L - 1);
+    const size_t M = (size_t)n * speclen;
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    int launches = 0;
+    if (M >= 0x80000000ull) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^31 ions in one length");
+
+    // entries: upload in SoA, sort by mass (or keep the given order)
+    std::vector<float> hm(n);
+    std::vector<uint32_t> hs(n), hmod(n);
+    std::vector<uint64_t> hsite(n);
+    for (uint32_t i = 0; i < n; i++)
+    {
+        hm[i] = h_entries[i].mass;
+        hs[i] = h_entries[i].seqid;
+        hsite[i] = h_entries[i].sites;
+        hmod[i] = h_entries[i].modnum;
+    }
+    float *d_m0 = nullptr;
+    uint32_t *d_s0 = nullptr, *d_mod0 = nullptr;
+    uint64_t *d_site0 = nullptr;
+    HC_CUDA(ctx, dalloc(&lh.d_mass, n));
+    HC_CUDA(ctx, dalloc(&lh.d_seqid, n));
+    HC_CUDA(ctx, dalloc(&lh.d_sites, n));
+    HC_CUDA(ctx, dalloc(&lh.d_modnum, n));
+    HC_CUDA(ctx, dalloc(&lh.d_bA, (size_t)nb + 1));
+    HC_CUDA(ctx, dalloc(&lh.d_iA, M));
+
+    // scratch: keys/vals ping-pong, radix histograms, scan temp
+    const size_t items = M > n ? M : n;
+    const size_t ntiles = (items + kRsTile - 1) / kRsTile;
+    uint32_t *k0, *k1, *v0, *v1, *hist, *stmp, *d_uninit;
+    HC_CUDA(ctx, dalloc(&k0, items));
+    HC_CUDA(ctx, dalloc(&k1, items));
+    HC_CUDA(ctx, dalloc(&v0, items));
+    HC_CUDA(ctx, dalloc(&v1, items));
+    HC_CUDA(ctx, dalloc(&hist, ntiles * kRadix));
+    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words(ntiles * kRadix)));
+    HC_CUDA(ctx, dalloc(&d_uninit, 1));
+    HC_CUDA(ctx, cudaMemsetAsync(d_uninit, 0, 4, st));
+
+    if (sort_by_mass && n > 1)
+    {
+        HC_CUDA(ctx, dalloc(&d_m0, n));
+        HC_CUDA(ctx, dalloc(&d_s0, n));
+        HC_CUDA(ctx, dalloc(&d_mod0, n));
+        HC_CUDA(ctx, dalloc(&d_site0, n));
+        HC_CUDA(ctx, cudaMemcpyAsync(d_m0, hm.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(d_s0, hs.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(d_mod0, hmod.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(d_site0, hsite.data(), 8ull * n, cudaMemcpyHostToDevice, st));
+        k_mass_keys<<<(n + 255) / 256, 256, 0, st>>>(d_m0, n, k0);
+        int which = 0;
+        HC_CUDA(ctx, radix_sort(k0, k1, nullptr, v1, n, 32, hist, stmp, st, &which, &launches, false));
+        // after an even number of passes the result is in (k0, v0)
+        uint32_t *perm = which ? v1 : v0;
+        k_gather_entries<<<(n + 255) / 256, 256, 0, st>>>(perm, n, d_m0, d_s0, d_site0, d_mod0,
+                                                          lh.d_mass, lh.d_seqid, lh.d_sites,
+                                                          lh.d_modnum);
+        launches += 2;
+    }
+    else
+    {
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_mass, hm.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_seqid, hs.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_modnum, hmod.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_sites, hsite.data(), 8ull * n, cudaMemcpyHostToDevice, st));
+    }
+
+    // ion keys -> (k0), sorted with ids -> iA, bucket bounds -> bA
+    if (M > 0)
+    {
+        const uint64_t threads = (uint64_t)n * 2 * ctx->p.maxz;
+        k_ion_keys<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+            ctx->d_tables, L, n, lh.d_mass, lh.d_seqid, lh.d_sites, lh.d_modnum, lh.d_seqs, k0,
+            d_uninit);
+        launches++;
+        int bits = 1;
+        while ((1ull << bits) < nb) bits++;
+        int which = 0;
+        HC_CUDA(ctx, radix_sort(k0, k1, nullptr, v1, M, bits, hist, stmp, st, &which, &launches, true));
+        uint32_t *skeys = which ? k1 : k0;
+        uint32_t *svals = which ? v1 : v0;
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_iA, svals, 4 * M, cudaMemcpyDeviceToDevice, st));
+        k_bucket_bounds<<<(unsigned)((M + 1 + 255) / 256), 256, 0, st>>>(skeys, M, nb, lh.d_bA);
+        launches += 2;
+    }
+    else
+    {
+        HC_CUDA(ctx, cudaMemsetAsync(lh.d_bA, 0, 4ull * (nb + 1), st));
+    }
+    uint32_t h_uninit = 0;
+    HC_CUDA(ctx, cudaMemcpyAsync(&h_uninit, d_uninit, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    cudaFree(k0);
+    cudaFree(k1);
+    cudaFree(v0);
+    cudaFree(v1);
+    cudaFree(hist);
+    cudaFree(stmp);
+    cudaFree(d_uninit);
+    if (d_m0)
+    {
+        cudaFree(d_m0);
+        cudaFree(d_s0);
+        cudaFree(d_mod0);
+        cudaFree(d_site0);
+    }
+    lh.npost = M;
+    lh.built = true;
+    ctx->lens_dirty = true;
+    ctx->last_launches = launches;
+    return HC_SUCCESS;
+}
+
+}  // namespace hc

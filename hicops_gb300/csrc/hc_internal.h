@@ -1,0 +1,140 @@
+// Internal declarations shared by the host API (hc_api.cpp) and the device
+// code (hc_index.cu, hc_query.cu). Not installed; not part of the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "hicops_gb300.h"
+
+namespace hc {
+
+constexpr int kMaxZ = 8;           // fragment charges handled (the reference clamps maxz <= 5)
+constexpr int kLgTable = 256;      // lgfact entries kept on the device (flagged past 80)
+constexpr int kRefMaxShp = 81;     // MAX_SHDPEAKS + 1 (utils.h:110)
+
+// One peptide length's device-resident index. All arrays are device pointers.
+struct LenDev
+{
+    uint32_t L, speclen, half, n;  // n = entries
+    uint32_t npep;
+    uint32_t magic, msh;           // floor(x / speclen) = umulhi(x, magic) >> msh, x < 2^31
+    uint32_t pad;
+    const float *mass;
+    const uint32_t *seqid;
+    const uint64_t *sites;
+    const uint32_t *modnum;
+    const uint8_t *seqs;
+    const uint32_t *bA;
+    const uint32_t *iA;
+};
+
+// Integer ion-key tables, derived on the host with the reference's double
+// arithmetic (utils.cpp:231-276 and 378-505; see hc_host.cpp).
+struct IonTables
+{
+    uint32_t bf[26][kMaxZ];   // (uint)((GETAA(a, z+1) * scale) / (z+1))
+    uint32_t yf[26][kMaxZ];   // (uint)(((GETAA(a, z+1) + H2O) * scale) / (z+1))
+    uint32_t inc[26][kMaxZ];  // (uint)((GETAA(a, 0) * scale) / (z+1))
+    uint32_t bfm[26][kMaxZ];  // (uint)(GETAA(a, z+1) * scale)          (mod spectra)
+    uint32_t yfm[26][kMaxZ];  // (uint)((GETAA(a, z+1) + H2O) * scale)  (mod spectra)
+    uint32_t incm[26];        // (uint)(GETAA(a, 0) * scale)             (mod spectra)
+    uint32_t mod_mass[16];
+    uint32_t maxz, scale, min_mass, max_mass;
+};
+
+struct QueryConst
+{
+    double lgfact[kLgTable];   // log10(n!) exactly as utils.h:115-131 builds it
+    float lgfact_f[kLgTable];  // the same, rounded to float (fast path)
+};
+
+// Host-side record of one length.
+struct LenHost
+{
+    uint32_t L = 0, npep = 0, n = 0;
+    uint64_t npost = 0;
+    float *d_mass = nullptr;
+    uint32_t *d_seqid = nullptr;
+    uint64_t *d_sites = nullptr;
+    uint32_t *d_modnum = nullptr;
+    uint8_t *d_seqs = nullptr;
+    uint32_t *d_bA = nullptr;
+    uint32_t *d_iA = nullptr;
+    bool built = false;
+};
+
+// Device scratch for one query call; grown on demand.
+struct QueryScratch
+{
+    int2 *d_win = nullptr;        // nspec * nlen windows [minl, maxl]
+    uint32_t *d_wide = nullptr;   // spectra that overflowed the packed scorecard
+    uint32_t *d_nwide = nullptr;
+    uint32_t *d_work = nullptr;   // work-stealing counter
+    size_t win_cap = 0, wide_cap = 0;
+    // host-path staging
+    void *d_in = nullptr;
+    size_t in_cap = 0;
+    void *d_outbuf = nullptr;
+    size_t out_cap = 0;
+};
+
+struct Launch
+{
+    uint32_t threads, tile, ctas_per_sm, pairs_per_warp;
+    size_t smem;
+    int grid;
+};
+
+}  // namespace hc
+
+struct hc_ctx
+{
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    hc_params p{};
+    cudaStream_t stream = nullptr;
+    hc_tuning tuning{};
+    std::vector<hc::LenHost> lens;
+    hc::LenDev *d_lens = nullptr;
+    hc::IonTables tables{};
+    hc::IonTables *d_tables = nullptr;
+    hc::QueryConst *d_qconst = nullptr;
+    hc::QueryScratch qs;
+    std::string last_error;
+    int last_launches = 0;
+    bool lens_dirty = true;
+};
+
+namespace hc {
+
+// hc_host.cpp
+void make_ion_tables(const hc_params &p, IonTables *t);
+void make_query_const(QueryConst *q);
+int64_t make_entries(const hc_params &p, uint32_t L, const uint8_t *seqs, uint32_t npep,
+                     hc_entry *out, int64_t cap);
+void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
+
+// hc_index.cu
+int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
+
+// hc_query.cu
+int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
+                 const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                 hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);
+int sync_lengths(hc_ctx *ctx);
+
+int set_error(hc_ctx *ctx, int code, const std::string &msg);
+int cuda_check(hc_ctx *ctx, cudaError_t e, const char *what);
+
+}  // namespace hc
+
+#define HC_CUDA(ctx, call)                                          \
+    do {                                                            \
+        cudaError_t _e = (call);                                    \
+        if (_e != cudaSuccess) return hc::cuda_check((ctx), _e, #call); \
+    } while (0)

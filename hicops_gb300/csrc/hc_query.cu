@@ -1,0 +1,806 @@
+// DSLIM query on the device (DSLIM_QuerySpectrum, source/core/dslim_query.cpp:515-842).
+//
+// Kernels, in launch order:
+//   k_windows   one thread per (spectrum, length): the precursor window
+//               [minlimit, maxlimit] of DSLIM_BinarySearch (dslim_query.cpp:854-994).
+//   k_search    persistent CTAs, one spectrum at a time (work stealing):
+//               for every length with a non-empty window, the candidate range
+//               is cut into shared-memory scorecard tiles; the postings of every
+//               (peak, bin) pair (dslim_query.cpp:617-676) are streamed with
+//               coalesced loads from a per-pair cursor, and each posting adds
+//               (count, intensity) to its candidate's packed 64-bit scorecard
+//               word with one shared-memory atomic. A candidate enters the
+//               qualifying list the moment its shared-peak count reaches
+//               min_shp; listed candidates are scored (dslim_query.cpp:679-725)
+//               into the 1002-bin histogram, cpsms and the top hit.
+//   k_search<WIDE> the same for spectra whose packed words could overflow
+//               (a count past 127): 2 x 64-bit words per candidate, exact FP64.
+//   k_tailfit   one thread per spectrum: expeRT::ModelTailFit (expeRT.cpp:572-718)
+//               and e(x) = 10^(mu*maxhyp + beta) * cpsms (dslim_query.cpp:773-799).
+//
+// Hyperscore. The reference evaluates h = lgfact[bc] + lgfact[yc] +
+// log10(1+ibc) + log10(1+iyc) - 6 in double and stores it as float. Here it is
+// first evaluated in float; the float value lies within 1.1e-4 of the
+// reference's (table rounding 2 x 7.6e-6, three float additions 3 x 1.6e-5,
+// log10f within 2 ulp, the final rounding 4e-6). Wherever that bound leaves a
+// decision open (sign, histogram bin, or a candidate that can still be the
+// top hit) the reference's double expression is evaluated, so cpsms, the
+// histogram and the top hit equal the reference's double evaluation.
+#include <cfloat>
+#include <cstring>
+#include <cstdio>
+
+#include "hc_internal.h"
+
+namespace hc {
+namespace {
+
+constexpr int kQcap = 2048;         // qualifying-candidate list per tile
+constexpr float kApproxErr = 1.1e-4f;
+constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
+constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
+
+struct SearchArgs
+{
+    const LenDev *lens;
+    uint32_t nlen;
+    const QueryConst *qc;
+    const uint32_t *idx, *moz, *inten;
+    const float *prec;
+    const int2 *win;
+    uint32_t nspec;
+    uint32_t dF, thr, min_shp, maxbin;  // maxbin = max_mass*scale
+    hc_result *out;
+    uint32_t *hist;
+    uint32_t *wide_list, *nwide;
+    uint32_t *work;
+    uint32_t tile;
+    const uint32_t *only;   // optional list of spectra to process (wide pass)
+    uint32_t nonly;
+};
+
+__device__ __forceinline__ uint32_t lower_bound_g(const uint32_t *__restrict__ a, uint32_t lo,
+                                                  uint32_t hi, uint32_t v)
+{
+    while (lo < hi)
+    {
+        uint32_t m = lo + ((hi - lo) >> 1);
+        if (__ldg(a + m) < v) lo = m + 1;
+        else hi = m;
+    }
+    return lo;
+}
+
+// The reference's double-precision hyperscore, rounded to float
+// (dslim_query.cpp:695-698). Additions only: no contraction possible.
+__device__ __forceinline__ float exact_h(const QueryConst *__restrict__ qc, uint32_t bc, uint32_t yc,
+                                        uint64_t ib, uint64_t iy)
+{
+    const double h1 = __dadd_rn(qc->lgfact[bc < kLgTable ? bc : kLgTable - 1],
+                                qc->lgfact[yc < kLgTable ? yc : kLgTable - 1]);
+    double h = __dadd_rn(h1, log10((double)(1 + ib)));
+    h = __dadd_rn(h, log10((double)(1 + iy)));
+    h = __dadd_rn(h, -6.0);
+    return (float)h;
+}
+
+// histogram bin (int)(h*10 + 0.5): a float product, then a double sum
+__device__ __forceinline__ int hist_bin(float hf)
+{
+    const float t = __fmul_rn(hf, 10.0f);
+    return (int)__dadd_rn((double)t, 0.5);
+}
+
+template <bool WIDE>
+struct Card;
+
+template <>
+struct Card<false>
+{
+    // [bc:8 | yc:8 | ibc:24 | iyc:24]; counts are kept below 128 (checked per
+    // posting), so with intensities < 2^17 the sums stay below 2^24.
+    using word = unsigned long long;
+    static constexpr int kWords = 1;
+};
+
+template <>
+struct Card<true>
+{
+    // b word and y word: [count:24 | sum:40]
+    using word = unsigned long long;
+    static constexpr int kWords = 2;
+};
+
+struct SmemTail
+{
+    uint32_t hist[HC_HIST_BINS];
+    uint32_t pad0[2];
+    unsigned long long best;   // (exact h bits << 32) | ~(ixx << 24 | psid)
+    uint32_t best_shp;
+    uint32_t maxbits;          // running max of the float estimate
+    uint32_t cpsms;
+    uint32_t qcount;
+    uint32_t flags;
+    uint32_t overflow;
+    uint32_t spec;
+    uint32_t nv;
+    unsigned long long bytes;
+    float lgf[kLgTable];
+};
+
+struct SmemLayout
+{
+    size_t qual, pcur, pend, pmoz, pint, tail, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide)
+{
+    const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
+    SmemLayout o;
+    o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
+    o.pcur = o.qual + 4ull * kQcap;
+    o.pend = o.pcur + 4 * maxpairs;
+    o.pmoz = o.pend + 4 * maxpairs;
+    o.pint = o.pmoz + 4ull * HC_QALEN;
+    o.tail = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
+    o.total = o.tail + sizeof(SmemTail);
+    return o;
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(1024) k_search(SearchArgs a)
+{
+    using W = typename Card<WIDE>::word;
+    constexpr int NW = Card<WIDE>::kWords;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tile = a.tile;
+    const uint32_t nbin = 2 * a.dF + 1;
+    const SmemLayout L = smem_layout(tile, a.dF, WIDE);
+    W *card = reinterpret_cast<W *>(smem);
+    uint32_t *qual = reinterpret_cast<uint32_t *>(smem + L.qual);
+    uint32_t *pcur = reinterpret_cast<uint32_t *>(smem + L.pcur);
+    uint32_t *pend = reinterpret_cast<uint32_t *>(smem + L.pend);
+    uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
+    uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
+    SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
+
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+
+    for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
+    for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
+
+    for (;;)
+    {
+        __syncthreads();
+        if (tid == 0)
+        {
+            uint32_t w = atomicAdd(a.work, 1u);
+            T.spec = a.only ? (w < a.nonly ? a.only[w] : 0xFFFFFFFFu) : (w < a.nspec ? w : 0xFFFFFFFFu);
+        }
+        for (int i = tid; i < HC_HIST_BINS; i += nthr) T.hist[i] = 0;
+        __syncthreads();
+        const uint32_t s = T.spec;
+        if (s == 0xFFFFFFFFu) break;
+        if (tid == 0)
+        {
+            T.best = 0;
+            T.best_shp = 0;
+            T.maxbits = 0;
+            T.cpsms = 0;
+            T.qcount = 0;
+            T.flags = WIDE ? HC_FLAG_WIDE : 0u;
+            T.overflow = 0;
+            T.bytes = 0;
+            T.nv = 0;
+        }
+        __syncthreads();
+        // valid peaks (dslim_query.cpp:625): dF < qion < max*scale - 1 - dF
+        {
+            const uint32_t p0 = a.idx[s], p1 = a.idx[s + 1];
+            for (uint32_t k = p0 + tid; k < p1; k += nthr)
+            {
+                const uint32_t q = a.moz[k];
+                if (q > a.dF && (uint64_t)q + 1 + a.dF < a.maxbin)
+                {
+                    // packed sums stay exact only for intensities below 2^17
+                    if (!WIDE && a.inten[k] >= (1u << 17)) T.overflow = 1;
+                    const uint32_t slot = atomicAdd(&T.nv, 1u);
+                    if (slot < HC_QALEN)
+                    {
+                        pmoz[slot] = q;
+                        pint[slot] = a.inten[k];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t nv = T.nv < HC_QALEN ? T.nv : HC_QALEN;
+        const uint32_t np = nv * nbin;
+        unsigned long long my_best = 0;
+        uint32_t my_shp = 0;
+
+        for (uint32_t l = 0; l < a.nlen; l++)
+        {
+            const int2 w = a.win[(size_t)s * a.nlen + l];
+            if (w.x > w.y) continue;
+            const LenDev d = a.lens[l];
+            const uint32_t lo_id = (uint32_t)w.x * d.speclen;
+            const uint32_t hi_id = (uint32_t)(w.y + 1) * d.speclen;
+            uint32_t my_bytes = 0;
+            for (uint32_t pr = tid; pr < np; pr += nthr)
+            {
+                const uint32_t k = pr / nbin, j = pr - k * nbin;
+                const uint32_t bin = pmoz[k] - a.dF + j;
+                const uint32_t st = __ldg(d.bA + bin), en = __ldg(d.bA + bin + 1);
+                uint32_t c = st, e = st;
+                if (en > st)
+                {
+                    c = (__ldg(d.iA + st) >= lo_id) ? st : lower_bound_g(d.iA, st + 1, en, lo_id);
+                    e = (__ldg(d.iA + en - 1) < hi_id) ? en : lower_bound_g(d.iA, c, en, hi_id);
+                }
+                pcur[pr] = c;
+                pend[pr] = e;
+                my_bytes += e - c;
+            }
+            if (my_bytes) atomicAdd(&T.bytes, 4ull * my_bytes);
+            if (tid == 0) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);
+            __syncthreads();
+
+            for (uint32_t c0 = (uint32_t)w.x; c0 <= (uint32_t)w.y; c0 += tile)
+            {
+                const uint32_t c1 = min(c0 + tile, (uint32_t)w.y + 1);
+                const uint32_t tile_hi = c1 * d.speclen;
+                // ---- stream postings into the scorecard tile ----
+                for (uint32_t pr = warp; pr < np; pr += nwarps)
+                {
+                    uint32_t cur = pcur[pr];
+                    const uint32_t end = pend[pr];
+                    const uint32_t intn = pint[pr / nbin];
+                    while (cur < end)
+                    {
+                        const uint32_t i = cur + lane;
+                        const uint32_t id = (i < end) ? __ldg(d.iA + i) : 0xFFFFFFFFu;
+                        const bool take = id < tile_hi;
+                        const uint32_t m = __ballot_sync(0xFFFFFFFFu, take);
+                        if (take)
+                        {
+                            const uint32_t ppid = __umulhi(id, d.magic) >> d.msh;
+                            const uint32_t loc = ppid - c0;
+                            const bool isY = (id - ppid * d.speclen) >= d.half;
+                            if (loc >= c1 - c0)
+                            {   // only an unsorted bucket can land here; never index past the tile
+                                T.overflow = 1;
+                            }
+                            else if constexpr (!WIDE)
+                            {
+                                const W add = isY ? ((1ull << 48) | (W)intn)
+                                                  : ((1ull << 56) | ((W)intn << 24));
+                                const W old = atomicAdd(&card[loc], add);
+                                const uint32_t cb = (uint32_t)(old >> 56), cy = (uint32_t)(old >> 48) & 0xFF;
+                                if ((isY ? cy : cb) >= 127u) T.overflow = 1;
+                                if (cb + cy + 1 == a.thr)
+                                {
+                                    const uint32_t qi = atomicAdd(&T.qcount, 1u);
+                                    if (qi < kQcap) qual[qi] = loc;
+                                }
+                            }
+                            else
+                            {
+                                // candidates are found by scanning the tile below
+                                atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)intn);
+                            }
+                        }
+                        const uint32_t cnt = __popc(m);
+                        cur += cnt;
+                        if (cnt < 32) break;
+                    }
+                    if (lane == 0) pcur[pr] = cur;
+                }
+                __syncthreads();
+                // ---- score the candidates that reached min_shp ----
+                const uint32_t qn = T.qcount;
+                const bool scan_all = WIDE || qn > (uint32_t)kQcap || a.thr > 250;
+                const uint32_t nscore = scan_all ? (c1 - c0) : qn;
+                for (uint32_t i = tid; i < nscore; i += nthr)
+                {
+                    const uint32_t loc = scan_all ? i : qual[i];
+                    uint32_t bc, yc;
+                    uint64_t ib, iy;
+                    if constexpr (!WIDE)
+                    {
+                        const W wd = card[loc];
+                        bc = (uint32_t)(wd >> 56);
+                        yc = (uint32_t)(wd >> 48) & 0xFF;
+                        ib = (wd >> 24) & 0xFFFFFF;
+                        iy = wd & 0xFFFFFF;
+                    }
+                    else
+                    {
+                        const W wb = card[2 * loc], wy = card[2 * loc + 1];
+                        bc = (uint32_t)(wb >> 40);
+                        yc = (uint32_t)(wy >> 40);
+                        ib = wb & 0xFFFFFFFFFFull;
+                        iy = wy & 0xFFFFFFFFFFull;
+                    }
+                    // reference reads bc/yc through short/ushort (dslim_query.cpp:684-686)
+                    const uint32_t shp = (uint32_t)(uint16_t)(bc + yc);
+                    if (shp < a.min_shp || shp == 0) continue;
+                    float hf;
+                    bool pos;
+                    int bin;
+                    bool exact = WIDE;
+                    float ha = 0.0f;
+                    if (!exact)
+                    {
+                        ha = ((T.lgf[bc] + T.lgf[yc]) + log10f((float)(1 + ib))) + log10f((float)(1 + iy)) - 6.0f;
+                        const float t = ha * 10.0f + 0.5f;
+                        const float fr = t - floorf(t);
+                        if (fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin)
+                            exact = true;
+                        else
+                        {
+                            pos = ha > 0.0f;
+                            bin = (int)floorf(t);
+                            hf = ha;
+                        }
+                    }
+                    if (exact)
+                    {
+                        hf = exact_h(a.qc, bc, yc, ib, iy);
+                        pos = hf > 0.0f;
+                        bin = hist_bin(hf);
+                        ha = hf;
+                    }
+                    if (!pos) continue;
+                    atomicAdd(&T.cpsms, 1u);
+                    uint32_t fl = 0;
+                    if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) fl |= HC_FLAG_LGFACT_OOB;
+                    if (bin >= HC_HIST_BINS || bin < 0) { fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
+                    if (fl) atomicOr(&T.flags, fl);
+                    atomicAdd(&T.hist[bin], 1u);
+                    // top-hit tracking: exact value for anything near the running max
+                    const uint32_t hb = __float_as_uint(ha);
+                    const uint32_t oldmax = atomicMax(&T.maxbits, hb);
+                    const float runmax = fmaxf(__uint_as_float(oldmax), ha);
+                    if (ha >= runmax - kNear)
+                    {
+                        const float he = WIDE ? hf : exact_h(a.qc, bc, yc, ib, iy);
+                        const uint32_t psid = c0 + loc;
+                        const uint32_t tie = (l << 24) | (psid & 0xFFFFFF);
+                        const unsigned long long key =
+                            ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
+                        if (key > my_best)
+                        {
+                            my_best = key;
+                            my_shp = shp;
+                        }
+                        atomicMax(&T.best, key);
+                    }
+                }
+                __syncthreads();
+                if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
+                // ---- clear the tile ----
+                {
+                    const uint32_t nw = (c1 - c0) * NW;
+                    uint4 *c4 = reinterpret_cast<uint4 *>(card);
+                    const uint32_t n4 = (nw + 1) / 2;
+                    for (uint32_t i = tid; i < n4; i += nthr) c4[i] = make_uint4(0, 0, 0, 0);
+                }
+                if (tid == 0) T.qcount = 0;
+                __syncthreads();
+            }
+        }
+        // ---- write the spectrum's results ----
+        if (!WIDE && T.overflow)
+        {
+            if (tid == 0)
+            {
+                const uint32_t wi = atomicAdd(a.nwide, 1u);
+                a.wide_list[wi] = s;
+            }
+            continue;
+        }
+        for (int i = tid; i < HC_HIST_BINS; i += nthr) a.hist[(size_t)s * HC_HIST_BINS + i] = T.hist[i];
+        if (tid == 0)
+        {
+            hc_result r;
+            r.cpsms = T.cpsms;
+            r.flags = T.flags;
+            r.post_bytes = T.bytes;
+            if (T.cpsms > 0 && T.best != 0)
+            {
+                const uint32_t tie = ~(uint32_t)(T.best & 0xFFFFFFFFu);
+                r.idxoffset = (int32_t)(tie >> 24);
+                r.psid = (int32_t)(tie & 0xFFFFFF);
+                r.hyperscore = __uint_as_float((uint32_t)(T.best >> 32));
+                r.sharedions = (uint16_t)T.best_shp;
+                r.totalions = (uint16_t)a.lens[r.idxoffset].speclen;
+            }
+            else
+            {
+                r.idxoffset = -1;
+                r.psid = -1;
+                r.hyperscore = 0.0f;
+                r.sharedions = 0;
+                r.totalions = 0;
+            }
+            r.mu = r.beta = r.minhyp = r.nexthyp = r.maxhyp = 0;
+            r.reported = 0;
+            r.evalue = 0.0;
+            a.out[s] = r;
+        }
+    }
+}
+
+// ---- windows: DSLIM_BinarySearch (dslim_query.cpp:854-994) -----------------
+__device__ int find_min(const float *__restrict__ m, float pm, int mn, int mx)
+{
+    for (;;)
+    {
+        int half = (mn + mx) / 2;
+        if (mx - mn < 20)
+        {
+            int cur = mn;
+            while (__ldg(m + cur) < pm) cur++;
+            return cur;
+        }
+        const float v = __ldg(m + half);
+        if (pm > v) { mn = half; continue; }
+        if (pm < v) { mx = half; continue; }
+        while (half >= 0 && pm == __ldg(m + half)) half--;
+        return half + 1;
+    }
+}
+
+__device__ int find_max(const float *__restrict__ m, int n, float pm, int mn, int mx)
+{
+    for (;;)
+    {
+        int half = (mn + mx) / 2;
+        if (mx - mn < 20)
+        {
+            int cur = mx;
+            while (__ldg(m + cur) > pm) cur--;
+            return cur;
+        }
+        const float v = __ldg(m + half);
+        if (pm > v) { mn = half; continue; }
+        if (pm < v) { mx = half; continue; }
+        half++;
+        while (half < n && pm == __ldg(m + half)) half++;
+        return half - 1;
+    }
+}
+
+__global__ void k_windows(const LenDev *__restrict__ lens, uint32_t nlen, const float *__restrict__ prec,
+                          const double *__restrict__ dMs, double dM0, uint32_t nspec, int2 *__restrict__ win)
+{
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint64_t)nspec * nlen) return;
+    const uint32_t s = (uint32_t)(g / nlen), l = (uint32_t)(g % nlen);
+    const double dM = dMs ? dMs[s] : dM0;
+    const float pm = prec[s];
+    // float pmass1 = precmass - params.dM: double difference rounded to float
+    const float pm1 = __double2float_rn(__dadd_rn((double)pm, -dM));
+    const float pm2 = __double2float_rn(__dadd_rn((double)pm, dM));
+    const int n = (int)lens[l].n;
+    const float *m = lens[l].mass;
+    int2 r = make_int2(1, 0);
+    if (n > 0 && !(dM < 0.0))
+    {
+        int mn = 0, mx = n - 1, lo, hi;
+        bool ok = true;
+        if (pm1 < __ldg(m + mn)) lo = mn;
+        else if (pm1 > __ldg(m + mx)) ok = false;
+        else lo = find_min(m, pm1, mn, mx);
+        if (ok)
+        {
+            if (pm2 > __ldg(m + mx)) hi = mx;
+            else if (pm2 < __ldg(m + mn)) ok = false;
+            else hi = find_max(m, n, pm2, mn, mx);
+        }
+        if (ok && __ldg(m + hi) <= pm2 && __ldg(m + lo) >= pm1 && hi >= lo) r = make_int2(lo, hi);
+    }
+    win[g] = r;
+}
+
+// ---- tail fit + e-value ------------------------------------------------------
+__device__ __forceinline__ int32_t x86_d2i(double v)
+{
+    // cvttsd2si semantics of the reference's double -> int conversions
+    if (!(v > -2147483649.0 && v < 2147483648.0)) return (int32_t)0x80000000u;
+    return (int32_t)v;
+}
+
+constexpr int kTfWarps = 4;
+
+// One warp per spectrum. Elementwise steps run across lanes; the sums whose
+// rounding depends on order (ybar, top, bot of LinearFit) run on lane 0 in
+// the reference's order. Cumulative sums are exact integers either way.
+__global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict__ out,
+                                                          const uint32_t *__restrict__ hist,
+                                                          uint32_t nspec, uint32_t min_cpsm,
+                                                          double expect_max)
+{
+    __shared__ double sxs[kTfWarps][HC_HIST_BINS + 2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t s = blockIdx.x * kTfWarps + warp;
+    if (s >= nspec) return;
+    double *sx = sxs[warp];  // sx[0] stands for index -1; element i is sx[i + 1]
+    hc_result r = out[s];
+    r.mu = r.beta = r.minhyp = r.nexthyp = r.maxhyp = 0;
+    r.evalue = 0.0;
+    r.reported = 0;
+    if (r.cpsms < min_cpsm || r.cpsms == 0)
+    {
+        if (lane == 0) out[s] = r;
+        return;
+    }
+    const uint32_t *yy = hist + (size_t)s * HC_HIST_BINS;
+    const int hyp = hist_bin(r.hyperscore);  // maxhypscore (dslim_query.cpp:778)
+    const int cps = (int)r.cpsms;
+    // expeRT.cpp:590-598: end1 = last bin below hyp holding >= 1, stt1 = first.
+    // Bins past the end exist only when the reference writes out of bounds
+    // (flagged HC_FLAG_HIST_OOB); they read as empty here.
+    int end1 = hyp - 1;
+    for (int q0 = min(hyp - 1, HC_HIST_BINS - 1); q0 >= 0; q0 -= 32)
+    {
+        const int q = q0 - lane;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, q >= 0 && yy[q] >= 1u);
+        if (b) { end1 = q0 - (__ffs(b) - 1); break; }
+    }
+    int stt1 = 0;
+    for (int q0 = 0; q0 <= end1 && q0 < HC_HIST_BINS; q0 += 32)
+    {
+        const int q = q0 + lane;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, q <= end1 && q < HC_HIST_BINS && yy[q] >= 1u);
+        if (b) { stt1 = q0 + __ffs(b) - 1; break; }
+    }
+    if (stt1 == end1) end1 += 1;
+    int n = end1 - stt1 + 1;
+    if (n < 0) n = 0;
+    if (stt1 + n > HC_HIST_BINS) n = HC_HIST_BINS - stt1;
+    double mu_t = 0.0, beta_t = 0.0;
+    uint32_t fl = 0;
+    if (n == 0)
+    {
+        fl |= HC_FLAG_TAILFIT_EMPTY;  // LinearFit of 0 points: 0/0
+        mu_t = beta_t = __longlong_as_double(0x7FF8000000000000ll);
+    }
+    else
+    {
+        // s(x) = -(cumsum/cpsms + -1), values > 1 -> 0.999 (expeRT.cpp:625-636)
+        unsigned long long carry = 0;
+        for (int i0 = 0; i0 < n; i0 += 32)
+        {
+            const int i = i0 + lane;
+            unsigned long long v = (i < n) ? yy[stt1 + i] : 0ull;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+                if (lane >= o) v += t;
+            }
+            if (i < n)
+            {
+                double d = __ddiv_rn((double)(carry + v), (double)cps);
+                d = -__dadd_rn(d, -1.0);
+                if (d > 1.0) d = 0.999;
+                sx[i + 1] = d;
+            }
+            carry += __shfl_sync(0xFFFFFFFFu, v, 31);
+        }
+        if (lane == 0) sx[0] = 0.0;
+        __syncwarp();
+        // values <= 0 take the last value >= 1e-4 (expeRT.cpp:639-640), then log10
+        int repl = n - 1;
+        for (int q0 = n - 1; q0 >= 0; q0 -= 32)
+        {
+            const int q = q0 - lane;
+            const uint32_t b = __ballot_sync(0xFFFFFFFFu, q >= 0 && sx[q + 1] >= 1e-4);
+            if (b) { repl = q0 - (__ffs(b) - 1); break; }
+        }
+        const double rv = sx[repl + 1];
+        __syncwarp();
+        for (int i = lane; i < n; i += 32)
+        {
+            double v = sx[i + 1];
+            if (v <= 0.0) v = rv;
+            sx[i + 1] = log10(v);
+        }
+        __syncwarp();
+        // regression window (expeRT.cpp:646-684)
+        int mark = 0, mark2 = n - 1;
+        const double hgt = __dadd_rn(sx[n], -sx[1]);
+        if (n >= 3)
+        {
+            const double t1 = __dadd_rn(sx[1], __dmul_rn(hgt, 0.22));
+            int lm = 0;
+            for (int q0 = 0; q0 < n; q0 += 32)
+            {
+                const int q = q0 + lane;
+                const uint32_t b = __ballot_sync(0xFFFFFFFFu, q < n && sx[q + 1] <= t1);
+                if (b) { lm = q0 + __ffs(b) - 1; break; }
+            }
+            mark = lm - 1;
+            if (n > 3)
+            {
+                const double t2 = __dadd_rn(sx[1], __dmul_rn(hgt, 0.87));
+                for (int q0 = n - 1; q0 >= 0; q0 -= 32)
+                {
+                    const int q = q0 - lane;
+                    const uint32_t b = __ballot_sync(0xFFFFFFFFu, q >= 0 && sx[q + 1] >= t2);
+                    if (b) { mark2 = q0 - (__ffs(b) - 1); break; }
+                }
+            }
+            if (mark >= mark2) mark = mark2 - 1;
+        }
+        if (mark < 0) fl |= HC_FLAG_TAILFIT_OOB;  // reads element -1 (sx[0] = +0.0)
+        const int m = mark2 - mark + 1;
+        const double *y = sx + 1 + mark;
+        // LinearFit (expeRT.cpp:1297-1345) on lane 0, in the reference's order
+        if (lane == 0)
+        {
+            if (m == 1)
+            {
+                mu_t = 0.0;
+                beta_t = y[0];
+            }
+            else
+            {
+                double xbar = 0.0, ybar = 0.0, top = 0.0, bot = 0.0;
+                for (int i = 0; i < m; i++)
+                {
+                    xbar = __dadd_rn(xbar, (double)(stt1 + mark + i));
+                    ybar = __dadd_rn(ybar, y[i]);
+                }
+                xbar = __ddiv_rn(xbar, (double)m);
+                ybar = __ddiv_rn(ybar, (double)m);
+                for (int i = 0; i < m; i++)
+                {
+                    const double dx = __dadd_rn((double)(stt1 + mark + i), -xbar);
+                    top = __dadd_rn(top, __dmul_rn(dx, __dadd_rn(y[i], -ybar)));
+                    bot = __dadd_rn(bot, __dmul_rn(dx, dx));
+                }
+                mu_t = __ddiv_rn(top, bot);
+                beta_t = __dadd_rn(ybar, -__dmul_rn(mu_t, xbar));
+            }
+        }
+    }
+    if (lane != 0) return;
+    r.flags |= fl;
+    r.mu = x86_d2i(__dmul_rn(mu_t, 1e6));
+    r.beta = x86_d2i(__dmul_rn(beta_t, 1e6));
+    r.minhyp = stt1;
+    r.nexthyp = end1;
+    r.maxhyp = hyp;
+    // e(x) = 10^(w*maxhyp + b) * cpsms (dslim_query.cpp:786-799)
+    const double wv = __ddiv_rn((double)r.mu, 1e6), bv = __ddiv_rn((double)r.beta, 1e6);
+    const double lgs = __dadd_rn(__dmul_rn(wv, (double)hyp), bv);
+    double e = pow(10.0, lgs);
+    e = __dmul_rn(e, (double)r.cpsms);
+    r.evalue = e;
+    r.reported = e < expect_max ? 1u : 0u;
+    out[s] = r;
+}
+
+size_t search_smem(uint32_t tile, uint32_t dF, bool wide) { return smem_layout(tile, dF, wide).total; }
+
+}  // namespace
+
+int sync_lengths(hc_ctx *ctx)
+{
+    if (!ctx->lens_dirty) return HC_SUCCESS;
+    const uint32_t nlen = (uint32_t)ctx->lens.size();
+    std::vector<LenDev> h(nlen);
+    for (uint32_t i = 0; i < nlen; i++)
+    {
+        const LenHost &lh = ctx->lens[i];
+        LenDev &d = h[i];
+        std::memset(&d, 0, sizeof(d));
+        d.L = lh.L;
+        d.n = lh.built ? lh.n : 0;
+        d.npep = lh.npep;
+        d.speclen = 2 * ctx->p.maxz * (lh.L - 1);
+        d.half = d.speclen / 2;
+        division_magic(d.speclen, &d.magic, &d.msh);
+        d.mass = lh.d_mass;
+        d.seqid = lh.d_seqid;
+        d.sites = lh.d_sites;
+        d.modnum = lh.d_modnum;
+        d.seqs = lh.d_seqs;
+        d.bA = lh.d_bA;
+        d.iA = lh.d_iA;
+    }
+    if (!ctx->d_lens) HC_CUDA(ctx, cudaMalloc((void **)&ctx->d_lens, sizeof(LenDev) * HC_MAX_LENGTHS));
+    HC_CUDA(ctx, cudaMemcpy(ctx->d_lens, h.data(), sizeof(LenDev) * nlen, cudaMemcpyHostToDevice));
+    ctx->lens_dirty = false;
+    return HC_SUCCESS;
+}
+
+template <class T>
+static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need)
+{
+    if (*cap >= need) return HC_SUCCESS;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    HC_CUDA(ctx, cudaMalloc((void **)p, sizeof(T) * need));
+    *cap = need;
+    return HC_SUCCESS;
+}
+
+int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
+                 const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                 hc_result *d_out, uint32_t *d_hist, cudaStream_t st)
+{
+    (void)npeaks;
+    int rc = sync_lengths(ctx);
+    if (rc) return rc;
+    ctx->last_launches = 0;
+    if (nspec == 0) return HC_SUCCESS;
+    const uint32_t nlen = (uint32_t)ctx->lens.size();
+    QueryScratch &q = ctx->qs;
+    if ((rc = grow(ctx, &q.d_win, &q.win_cap, (size_t)nspec * nlen))) return rc;
+    if ((rc = grow(ctx, &q.d_wide, &q.wide_cap, (size_t)nspec + 4))) return rc;
+    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 16));
+    q.d_nwide = q.d_work + 2;
+    HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 16, st));
+
+    const uint64_t nw = (uint64_t)nspec * nlen;
+    k_windows<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(ctx->d_lens, nlen, d_prec, d_dM, ctx->p.dM,
+                                                            nspec, q.d_win);
+    HC_CUDA(ctx, cudaGetLastError());
+
+    SearchArgs a{};
+    a.lens = ctx->d_lens;
+    a.nlen = nlen;
+    a.qc = ctx->d_qconst;
+    a.idx = d_idx;
+    a.moz = d_moz;
+    a.inten = d_int;
+    a.prec = d_prec;
+    a.win = q.d_win;
+    a.nspec = nspec;
+    a.dF = ctx->p.dF;
+    a.min_shp = ctx->p.min_shp;
+    a.thr = ctx->p.min_shp > 0 ? ctx->p.min_shp : 1;
+    a.maxbin = ctx->p.max_mass * ctx->p.scale;
+    a.out = d_out;
+    a.hist = d_hist;
+    a.wide_list = q.d_wide;
+    a.nwide = q.d_nwide;
+    a.work = q.d_work;
+    a.tile = ctx->tuning.tile;
+    const size_t smem = search_smem(a.tile, a.dF, false);
+    HC_CUDA(ctx, cudaFuncSetAttribute(k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
+    k_search<false><<<grid, ctx->tuning.threads, smem, st>>>(a);
+    HC_CUDA(ctx, cudaGetLastError());
+
+    // spectra whose packed scorecard could overflow: redo them wide
+    uint32_t nwide = 0;
+    HC_CUDA(ctx, cudaMemcpyAsync(&nwide, q.d_nwide, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    int launches = 2;
+    if (nwide > 0)
+    {
+        SearchArgs b = a;
+        b.only = q.d_wide;
+        b.nonly = nwide;
+        b.work = q.d_work + 1;
+        b.tile = ctx->tuning.tile / 2;
+        const size_t smem2 = search_smem(b.tile, b.dF, true);
+        HC_CUDA(ctx, cudaFuncSetAttribute(k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        k_search<true><<<grid, ctx->tuning.threads, smem2, st>>>(b);
+        HC_CUDA(ctx, cudaGetLastError());
+        launches++;
+    }
+    k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
+                                                                            ctx->p.expect_max);
+    HC_CUDA(ctx, cudaGetLastError());
+    ctx->last_launches = launches + 1;
+    return HC_SUCCESS;
+}
+
+}  // namespace hc

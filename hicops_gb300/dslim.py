@@ -1,0 +1,156 @@
+"""Reference-facing host interface of the GB300 DSLIM search.
+
+Mirrors the reference's DSLIM entry points (source/core/include/dslim.h) on
+top of the C ABI: ``DSLIM_Construct`` builds one peptide length's index on the
+device, ``DSLIM_QuerySpectrum`` searches a CSR batch (the ``Queries`` layout,
+slm_dsts.h:422-559) and returns, per spectrum, what the reference hands to
+``DFile_PrintScore`` (dslim_fileout.cpp:112-152). Status codes follow
+slmerr.h; a failing call raises HcError carrying the code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .params import gParams
+
+
+class Index:
+    """Device-resident SLM index of all peptide lengths (the reference's Index[])."""
+
+    def __init__(self, params: gParams, device: int = 0):
+        self.params = params
+        self._cp = L.to_hc_params(params)
+        lib = L.load()
+        h = C.c_void_p()
+        rc = lib.hc_ctx_create(device, C.byref(self._cp), C.byref(h))
+        if rc != 0:
+            raise L.HcError(rc, "hc_ctx_create")
+        self.ctx = h
+        self.lib = lib
+        self.seqs: dict[int, np.ndarray] = {}
+
+    def close(self):
+        if self.ctx:
+            self.lib.hc_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise L.HcError(rc, what, self.lib.hc_last_error(self.ctx).decode())
+
+    # -- tuning --
+    def tuning(self) -> dict:
+        t = L.HcTuning()
+        self._check(self.lib.hc_ctx_get_tuning(self.ctx, C.byref(t)), "hc_ctx_get_tuning")
+        return {k: getattr(t, k) for k, _ in L.HcTuning._fields_}
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = L.HcTuning(**cur)
+        self._check(self.lib.hc_ctx_set_tuning(self.ctx, C.byref(t)), "hc_ctx_set_tuning")
+
+    # -- index --
+    def construct(self, L_: int, seqs: np.ndarray, order: np.ndarray | None = None):
+        """DSLIM_Construct for one length (dslim.h:49)."""
+        seqs = np.ascontiguousarray(seqs, dtype=np.uint8).reshape(-1, L_)
+        self.seqs[L_] = seqs
+        o = None if order is None else np.ascontiguousarray(order, dtype=L.ENTRY_DTYPE)
+        self._check(self.lib.hc_dslim_construct(self.ctx, L_, L.ptr(seqs), seqs.shape[0], L.ptr(o),
+                                                0 if o is None else o.shape[0]), "hc_dslim_construct")
+
+    def construct_all(self, db: dict, orders: dict | None = None):
+        for L_ in range(self.params.min_len, self.params.max_len + 1):
+            self.construct(L_, db.get(L_, np.zeros((0, L_), np.uint8)),
+                           None if orders is None else orders.get(L_))
+
+    def load(self, L_: int, seqs: np.ndarray, entries: np.ndarray, bA: np.ndarray, iA: np.ndarray):
+        """Load a host-built index as-is (bA/iA as the reference's DSLIM_Construct lays them out)."""
+        seqs = np.ascontiguousarray(seqs, dtype=np.uint8).reshape(-1, L_)
+        self.seqs[L_] = seqs
+        e = np.ascontiguousarray(entries, dtype=L.ENTRY_DTYPE)
+        bA = np.ascontiguousarray(bA, dtype=np.uint32)
+        iA = np.ascontiguousarray(iA, dtype=np.uint32)
+        self._check(self.lib.hc_dslim_load(self.ctx, L_, L.ptr(seqs), seqs.shape[0], L.ptr(e), e.shape[0],
+                                           L.ptr(bA), L.ptr(iA)), "hc_dslim_load")
+
+    def info(self, L_: int):
+        n = C.c_uint32()
+        m = C.c_uint64()
+        self._check(self.lib.hc_dslim_info(self.ctx, L_, C.byref(n), C.byref(m)), "hc_dslim_info")
+        return n.value, m.value
+
+    def export(self, L_: int):
+        n, m = self.info(L_)
+        e = np.zeros(n, dtype=L.ENTRY_DTYPE)
+        bA = np.zeros(self.params.max_mass * self.params.scale + 1, dtype=np.uint32)
+        iA = np.zeros(m, dtype=np.uint32)
+        self._check(self.lib.hc_dslim_export(self.ctx, L_, L.ptr(e), L.ptr(bA), L.ptr(iA)), "hc_dslim_export")
+        return e, bA, iA
+
+    def entries(self, L_: int) -> np.ndarray:
+        n, _ = self.info(L_)
+        e = np.zeros(n, dtype=L.ENTRY_DTYPE)
+        self._check(self.lib.hc_dslim_export(self.ctx, L_, L.ptr(e), None, None), "hc_dslim_export")
+        return e
+
+    # -- query --
+    def query(self, q, want_hist: bool = True):
+        """DSLIM_QuerySpectrum (dslim.h:184) on a host CSR batch; returns (results, hist)."""
+        n = q.nspec
+        out = np.zeros(n, dtype=L.RESULT_DTYPE)
+        hist = np.zeros((n, L.HC_HIST_BINS), dtype=np.uint32) if want_hist else None
+        idx = np.ascontiguousarray(q.idx, dtype=np.uint32)
+        moz = np.ascontiguousarray(q.moz, dtype=np.uint32)
+        inten = np.ascontiguousarray(q.intensity, dtype=np.uint32)
+        prec = np.ascontiguousarray(q.precurse, dtype=np.float32)
+        dM = None if getattr(q, "dM", None) is None else np.ascontiguousarray(q.dM, dtype=np.float64)
+        self._check(self.lib.hc_dslim_query(self.ctx, L.ptr(idx), L.ptr(moz), L.ptr(inten), L.ptr(prec),
+                                            L.ptr(dM), n, L.ptr(out), L.ptr(hist)), "hc_dslim_query")
+        return out, hist
+
+    def query_device(self, d_idx: int, d_moz: int, d_int: int, d_prec: int, d_dM: int | None, nspec: int,
+                     npeaks: int, d_out: int, d_hist: int, stream: int | None = None):
+        """Device-buffer query (raw device pointers); enqueued on `stream`."""
+        self._check(self.lib.hc_dslim_query_device(
+            self.ctx, C.c_void_p(d_idx), C.c_void_p(d_moz), C.c_void_p(d_int), C.c_void_p(d_prec),
+            None if d_dM is None else C.c_void_p(d_dM), nspec, npeaks, C.c_void_p(d_out),
+            C.c_void_p(d_hist), None if stream is None else C.c_void_p(stream)), "hc_dslim_query_device")
+
+    def last_launch_count(self) -> int:
+        return self.lib.hc_last_launch_count(self.ctx)
+
+    def identity(self, res: np.ndarray):
+        """(seqid, modnum, sites) of each top hit (-1 where none)."""
+        n = res.shape[0]
+        sid = np.full(n, -1, dtype=np.int64)
+        mod = np.zeros(n, dtype=np.uint32)
+        site = np.zeros(n, dtype=np.uint64)
+        cache = {}
+        for i in np.nonzero(res["idxoffset"] >= 0)[0]:
+            L_ = int(res["idxoffset"][i]) + self.params.min_len
+            if L_ not in cache:
+                cache[L_] = self.entries(L_)
+            e = cache[L_][int(res["psid"][i])]
+            sid[i], mod[i], site[i] = e["seqid"], e["modnum"], e["sites"]
+        return sid, mod, site
+
+
+def DSLIM_Construct(index: Index, L_: int, seqs: np.ndarray) -> int:
+    """dslim.h:49 — build one length's index on the device; returns SLM_SUCCESS."""
+    index.construct(L_, seqs)
+    return 0
+
+
+def DSLIM_QuerySpectrum(queries, index: Index):
+    """dslim.h:184 — search a batch; returns (results, histograms)."""
+    return index.query(queries)

@@ -32,6 +32,8 @@ import os
 
 import numpy as np
 
+from .params import gParams
+
 QALEN = 100
 PROTON = 1.00727647
 H2O_F32 = np.float32(18.015)
@@ -65,47 +67,13 @@ _KR = np.array([ord('K'), ord('R')], dtype=np.uint8)
 _KR_P = np.array([_NATURAL_FREQ['K'], _NATURAL_FREQ['R']]) / (_NATURAL_FREQ['K'] + _NATURAL_FREQ['R'])
 
 
-@dataclasses.dataclass
-class SearchParams:
-    """The gParams fields the DSLIM path reads (source/core/include/slm_dsts.h:359-418).
+class SearchParams(gParams):
+    """gParams with the defaults of the measured workloads (report everything)."""
 
-    ``dF`` is in bins (the reference stores (uint)(tolerance * 100),
-    source/app/hicops.cpp:564); ``dM`` in Da; ``mods`` is a list of
-    (residues, mass_Da, max_per_peptide) and ``vmods_per_pep`` the overall limit.
-    """
-    min_len: int = 7
-    max_len: int = 40
-    maxz: int = 3
-    topmatches: int = 10
-    scale: int = 100
-    min_shp: int = 4
-    min_cpsm: int = 4
-    min_mass: int = 500
-    max_mass: int = 5000
-    dF: int = 1
-    dM: float = 500.0
-    res: float = 0.01
-    expect_max: float = 1e300
-    base_int: int = 100000
-    min_int: int = 1000
-    threads: int = 8
-    spadmem: int = 2000000000
-    vmods_per_pep: int = 0
-    mods: list = dataclasses.field(default_factory=list)
-
-    def mod_mass_scaled(self, i: int) -> int:
-        """Scaled mod mass as stored by the parameter parser (source/app/hicops.cpp:661)."""
-        return int(np.floor(np.float64(self.mods[i][1]) * np.float64(self.scale)))
-
-    def write_ref_params(self, path: str) -> None:
-        with open(path, "w") as f:
-            for k in ("threads", "min_len", "max_len", "maxz", "topmatches", "scale",
-                      "min_shp", "min_cpsm", "spadmem", "min_mass", "max_mass", "dF",
-                      "base_int", "min_int", "vmods_per_pep"):
-                f.write(f"{k} {getattr(self, k)}\n")
-            f.write(f"dM {self.dM!r}\nres {self.res!r}\nexpect_max {self.expect_max!r}\n")
-            for res, mass, per in self.mods:
-                f.write(f"mod {res} {mass!r} {per}\n")
+    def __init__(self, **kw):
+        kw.setdefault("min_len", 7)
+        kw.setdefault("expect_max", 1e300)
+        super().__init__(**kw)
 
 
 def pep_mass_f32(seqs: np.ndarray) -> np.ndarray:

@@ -1,0 +1,166 @@
+/*
+ * hicops_gb300 — GB300 (sm_103a) DSLIM database peptide search: C ABI.
+ *
+ * Drop-in boundary for the HiCOPS DSLIM index/query path. The reference calls
+ * these C++ functions from its driver (source/app/hicops.cpp:287-340):
+ *
+ *   status_t DSLIM_Construct(Index *index);                     dslim.h:49
+ *   status_t DSLIM_InitializeScorecard(Index *index, uint_t n); dslim.h:53
+ *   status_t DSLIM_QuerySpectrum(Queries *ss, Index *index,
+ *                                uint_t idxchunk);              dslim.h:184
+ *   status_t DFile_PrintScore(Index*, uint_t specid, float_t pmass, hCell *psm,
+ *                             double_t e_x, uint_t npsms);      dslim_fileout.h:29
+ *
+ * and read the global gParams (slm_dsts.h:359-418). Here every call takes a
+ * context that owns the device-resident index, the parameters and the
+ * scratch, and returns the reference's status_t convention (slmerr.h:24-46:
+ * 0 = success, negative codes from -3001). Plain pointers and sizes only.
+ *
+ * Threading: one context per host thread; calls on one context are serialised
+ * by the caller. Device work runs on the stream given (or the context's own).
+ */
+#ifndef HICOPS_GB300_H
+#define HICOPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (slmerr.h:24-46) ---- */
+#define HC_SUCCESS 0
+#define HC_ERR_INVLD_MEMORY (-3001)
+#define HC_ERR_INVLD_PARAM (-3002)
+#define HC_ERR_INVLD_INDEX (-3003)
+#define HC_ERR_INVLD_SIZE (-3004)
+#define HC_ERR_BAD_MEM_ALLOC (-3007)
+#define HC_ERR_INVLD_PTR (-3008)
+#define HC_ERR_INVLD_MOD (-3010)
+#define HC_ERR_NOT_ENOUGH_DATA (-3012)
+/* codes without a reference counterpart */
+#define HC_ERR_CUDA (-3020)      /* a CUDA runtime call failed; see hc_last_error */
+#define HC_ERR_TIMEOUT (-3021)   /* a bounded device wait ran out */
+#define HC_ERR_NO_DEVICE (-3022) /* no CUDA device, or not an sm_103 part */
+
+#define HC_HIST_BINS 1002 /* 2 + MAX_HYPERSCORE*10 (dslim.cpp:419) */
+#define HC_QALEN 100      /* peaks per spectrum (config.hpp QALEN) */
+#define HC_MAX_MODS 15    /* MAX_MOD_TYPES (slm_dsts.h:28) */
+#define HC_MAX_LENGTHS 64
+
+/* per-spectrum result flags */
+#define HC_FLAG_LGFACT_OOB 0x1u    /* bc or yc > 80: the reference reads lgfact[] out of bounds */
+#define HC_FLAG_HIST_OOB 0x2u      /* hyperscore bin > 1001: out-of-bounds histogram write */
+#define HC_FLAG_TAILFIT_OOB 0x4u   /* tail-fit slice starts at -1 (expeRT.cpp:653,690) */
+#define HC_FLAG_TAILFIT_EMPTY 0x8u /* empty tail-fit slice: 0/0 fit (expeRT.cpp:590-601) */
+#define HC_FLAG_WIDE 0x100u        /* scored by the wide-scorecard kernel */
+
+/* gParams fields on the DSLIM path (slm_dsts.h:359-418). dF is in bins
+ * ((uint)(tolerance_Da * scale), hicops.cpp:564); dM in Da; mod_mass is scaled
+ * ((uint)(mass * scale), hicops.cpp:661). */
+typedef struct hc_params
+{
+    uint32_t min_len, max_len, maxz, topmatches, scale, min_shp, min_cpsm;
+    uint32_t min_mass, max_mass, dF;
+    int32_t base_int, min_int;
+    double dM, expect_max;
+    uint32_t nmods, vmods_per_pep;
+    uint32_t mod_mass[HC_MAX_MODS];
+    char mod_res[HC_MAX_MODS][4];
+    uint32_t mod_per_pep[HC_MAX_MODS];
+    uint32_t threads; /* host threads for host-side steps */
+} hc_params;
+
+/* One database entry: pepEntry (slm_dsts.h:146-282) with explicit padding. */
+typedef struct hc_entry
+{
+    float mass;
+    uint32_t seqid;
+    uint64_t sites;
+    uint32_t modnum;
+    uint32_t pad;
+} hc_entry;
+
+/* Per-spectrum search result: the fields DFile_PrintScore receives
+ * (dslim_fileout.cpp:112-152) plus the Results state (slm_dsts.h:694-754). */
+typedef struct hc_result
+{
+    uint32_t cpsms;       /* candidate PSMs with hyperscore > 0 */
+    int32_t idxoffset;    /* length index of the top hit (-1: none) */
+    int32_t psid;         /* entry index of the top hit inside that length */
+    uint16_t sharedions;  /* bc + yc of the top hit */
+    uint16_t totalions;   /* speclen of the top hit */
+    float hyperscore;     /* top hyperscore */
+    int32_t mu, beta;     /* tail-fit slope/intercept x 1e6 (expeRT.cpp:703-704) */
+    int32_t minhyp, nexthyp, maxhyp;
+    uint32_t flags;
+    uint32_t reported;    /* cpsms >= min_cpsm and evalue < expect_max */
+    double evalue;
+    uint64_t post_bytes;  /* algorithmic bytes: in-window postings + bucket reads */
+} hc_result;
+
+typedef struct hc_ctx hc_ctx;
+
+/* Query-kernel launch shape (chosen by hc_tune or set by the caller). */
+typedef struct hc_tuning
+{
+    uint32_t threads;      /* threads per CTA (multiple of 32, <= 1024) */
+    uint32_t tile;         /* scorecard candidates per shared-memory tile */
+    uint32_t ctas_per_sm;  /* resident CTAs per SM the grid is sized for */
+    uint32_t pairs_per_warp; /* (peak, bin) postings lists a warp streams at once */
+} hc_tuning;
+
+int hc_version(void);
+const char *hc_status_string(int status);
+
+/* ---- context (owns the index, the scorecard scratch and a stream) ---- */
+int hc_ctx_create(int device, const hc_params *p, hc_ctx **out);
+int hc_ctx_destroy(hc_ctx *ctx);
+const char *hc_last_error(const hc_ctx *ctx);
+int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t);
+int hc_ctx_get_tuning(const hc_ctx *ctx, hc_tuning *t);
+
+/* ---- index (DSLIM_Construct, dslim.h:49; LBE_Initialize, lbe.h) ----
+ * Builds the SLM index of one peptide length on the device: entries (base
+ * peptides in file order, then variable-mod variants, mods.cpp:333-496) are
+ * sorted by mass on the device (stable), ion keys are generated, and the
+ * bucket (bA) and postings (iA) arrays are built by a device radix sort.
+ * seqs: npep*L residues (already mass-filtered as LBE_CountPeps does,
+ * lbe_internal.cpp:413). order: optional entries in a caller-fixed order
+ * (e.g. the reference's own sorted order); NULL = device sort. */
+int hc_dslim_construct(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep,
+                       const hc_entry *order, uint32_t norder);
+/* Loads a host-built index as-is (bA/iA as DSLIM_Construct lays them out). */
+int hc_dslim_load(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep,
+                  const hc_entry *entries, uint32_t n, const uint32_t *bA, const uint32_t *iA);
+int hc_dslim_info(hc_ctx *ctx, uint32_t L, uint32_t *n_entries, uint64_t *n_postings);
+/* Copies one length's entries / bA (max_mass*scale+1) / iA back (any may be NULL). */
+int hc_dslim_export(hc_ctx *ctx, uint32_t L, hc_entry *entries, uint32_t *bA, uint32_t *iA);
+/* Enumerates a length's entries on the host exactly as hc_dslim_construct
+ * does before its device sort; returns the count (or a negative status).
+ * out may be NULL to count only. */
+int64_t hc_make_entries(const hc_params *p, uint32_t L, const uint8_t *seqs, uint32_t npep,
+                        hc_entry *out, int64_t cap);
+
+/* ---- query (DSLIM_QuerySpectrum, dslim.h:184) ----
+ * CSR batch in host memory: idx[nspec+1] offsets into moz/intensity;
+ * precurse[nspec]; dM_per_spec optional per-spectrum tolerance (Da, NULL =
+ * params.dM). out[nspec] results; hist optional nspec*1002 counts. */
+int hc_dslim_query(hc_ctx *ctx, const uint32_t *idx, const uint32_t *moz,
+                   const uint32_t *intensity, const float *precurse,
+                   const double *dM_per_spec, uint32_t nspec, hc_result *out, uint32_t *hist);
+/* Same, all buffers device-resident, enqueued on `stream` (cudaStream_t;
+ * NULL = the context stream). npeaks = idx[nspec]. Returns after enqueueing;
+ * the host does not wait. */
+int hc_dslim_query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz,
+                          const uint32_t *d_intensity, const float *d_precurse,
+                          const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                          hc_result *d_out, uint32_t *d_hist, void *stream);
+/* Kernel launches made by the last query call (for launch accounting). */
+int hc_last_launch_count(const hc_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HICOPS_GB300_H */

@@ -1,0 +1,127 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bit-exact: entries and their order, bA, iA, cpsms, histograms, top hit
+(length, psid, shared ions), hyperscore. Tail-fit ints mu/beta exact for
+>= 99 % of reported spectra and |delta log10 e| <= 0.05 for all (the device
+log10/pow may differ from the host's in the last bit).
+"""
+import numpy as np
+import pytest
+
+from tests._util import case, compare
+from hicops_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dslim():
+    from hicops_gb300 import dslim as D
+    return D
+
+
+@pytest.fixture(scope="module")
+def orc():
+    from oracle import oracle as O
+    return O
+
+
+@pytest.mark.parametrize("name,npep,nq,seed", [("plain", 3000, 300, 101), ("mods", 3000, 300, 202)])
+def test_index_bitexact(dslim, orc, name, npep, nq, seed):
+    p, db, q = case(name, npep, nq, seed)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    for L in range(p.min_len, p.max_len + 1):
+        e, bA, iA = ix.export(L)
+        oe = orc.make_entries(db[L], L, p)          # stable by mass, generation order
+        assert e.shape == oe.shape
+        assert np.array_equal(e.view(np.uint8), oe.view(np.uint8)), f"entries differ at L={L}"
+        obA, oiA = orc.build_index(db[L], L, oe, p)
+        assert np.array_equal(bA, obA), f"bA differs at L={L}"
+        assert np.array_equal(iA, oiA), f"iA differs at L={L}"
+    ix.close()
+
+
+@pytest.mark.parametrize("name,npep,nq,seed", [("plain", 3000, 400, 303), ("mods", 3000, 400, 404)])
+def test_query_parity(dslim, orc, name, npep, nq, seed):
+    p, db, q = case(name, npep, nq, seed)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    res, hist = ix.query(q)
+    oi = orc.OracleIndex(db, p)
+    ores, ohist = oi.query(q, tie_rule=1)
+    st = compare(res, hist, ores, ohist)
+    assert st["reported"] > 0
+    ix.close()
+
+
+def test_query_parity_loaded_index(dslim, orc):
+    """Query over a host-built index loaded as-is (hc_dslim_load)."""
+    p, db, q = case("mods", 2000, 200, 505)
+    oi = orc.OracleIndex(db, p)
+    ix = dslim.Index(p)
+    for L, d in oi.lengths.items():
+        ix.load(L, d["seqs"], d["entries"], d["bA"], d["iA"])
+    res, hist = ix.query(q)
+    ores, ohist = oi.query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
+def test_query_parity_mixed_windows(dslim, orc):
+    """Per-spectrum precursor tolerances (10 ppm / 50 Da / 500 Da)."""
+    p = S.SearchParams(maxz=3, dF=1, dM=500.0, threads=8, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+    db = S.make_database(3000, 606, p)
+    q = S.make_queries(db, 400, 607, p, peaks=(20, 150),
+                       window_mix=[(0.5, "ppm", 10.0), (0.3, "da", 50.0), (0.2, "da", 500.0)])
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    res, hist = ix.query(q)
+    ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
+def test_wide_path(dslim, orc):
+    """Intensities >= 2^17 cannot use the packed scorecard: the wide kernel must agree."""
+    p, db, q = case("plain", 2000, 200, 707, base_int=1000000, min_int=10000)
+    q2 = S.make_queries(db, 200, 708, p)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    res, hist = ix.query(q2)
+    assert (res["flags"] & 0x100).any(), "wide path not exercised"
+    ores, ohist = orc.OracleIndex(db, p).query(q2, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
+def test_small_tiles(dslim, orc):
+    """Many scorecard tiles per length (tile smaller than the windows)."""
+    p, db, q = case("mods", 3000, 200, 808)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    ix.set_tuning(tile=512, threads=256)
+    res, hist = ix.query(q)
+    ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
+def test_empty_and_edge_batches(dslim, orc):
+    p, db, q = case("plain", 1000, 50, 909)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    # empty batch
+    e = q.slice(0, 0)
+    r0, _ = ix.query(e)
+    assert r0.shape == (0,)
+    # spectra with no peaks, with a single peak, with peaks at the bin limits
+    nz = S.QueryBatch(idx=np.array([0, 0, 1, 4], np.uint32),
+                      moz=np.array([50000, 0, 2, 499998], np.uint32),
+                      intensity=np.array([100000, 5, 5, 5], np.uint32),
+                      precurse=np.array([1500.0, 1200.0, 2000.0], np.float32),
+                      charges=np.array([2, 2, 2], np.int32), rtimes=np.zeros(3, np.float32))
+    r, h = ix.query(nz)
+    orr, oh = orc.OracleIndex(db, p).query(nz, tie_rule=1)
+    compare(r, h, orr, oh)
+    ix.close()
