@@ -88,6 +88,10 @@ _SIGS = [
                                         C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),
     ("hc_last_launch_count", C.c_int, [C.c_void_p]),
+    ("hc_check_division", C.c_uint64, [C.c_uint32, C.c_uint32]),
+    ("hc_ctx_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
+    ("hc_last_kernel_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                       C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 ]
 
 EXPORTED = [s[0] for s in _SIGS]

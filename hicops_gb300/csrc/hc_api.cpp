@@ -141,6 +141,8 @@ int hc_ctx_destroy(hc_ctx *ctx)
     cudaFree(ctx->qs.d_work);
     cudaFree(ctx->qs.d_in);
     cudaFree(ctx->qs.d_outbuf);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HC_SUCCESS;
@@ -361,5 +363,40 @@ int hc_dslim_query(hc_ctx *ctx, const uint32_t *idx, const uint32_t *moz, const 
 }
 
 int hc_last_launch_count(const hc_ctx *ctx) { return ctx ? ctx->last_launches : -1; }
+
+uint64_t hc_check_division(uint32_t d, uint32_t xmax)
+{
+    if (d < 2) return 1;
+    uint32_t m, sh;
+    division_magic(d, &m, &sh);
+    uint64_t bad = 0;
+    for (uint32_t x = 0; x < xmax; x++)
+        if ((uint32_t)(((uint64_t)x * m) >> 32) >> sh != x / d) bad++;
+    return bad;
+}
+
+int hc_ctx_set_profiling(hc_ctx *ctx, int on)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    cudaSetDevice(ctx->device);
+    if (on && !ctx->ev[0])
+        for (auto &e : ctx->ev) HC_CUDA(ctx, cudaEventCreate(&e));
+    ctx->profiling = on != 0;
+    return HC_SUCCESS;
+}
+
+int hc_last_kernel_times(hc_ctx *ctx, float *ms_windows, float *ms_search, float *ms_wide, float *ms_tailfit)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    if (!ctx->profiling || !ctx->ev[0]) return set_error(ctx, HC_ERR_INVLD_PARAM, "profiling is off");
+    HC_CUDA(ctx, cudaEventSynchronize(ctx->ev[4]));
+    float t[4];
+    for (int i = 0; i < 4; i++) HC_CUDA(ctx, cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]));
+    if (ms_windows) *ms_windows = t[0];
+    if (ms_search) *ms_search = t[1];
+    if (ms_wide) *ms_wide = t[2];
+    if (ms_tailfit) *ms_tailfit = t[3];
+    return HC_SUCCESS;
+}
 
 }  // extern "C"

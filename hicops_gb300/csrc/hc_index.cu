@@ -192,15 +192,16 @@ size_t scan_tmp_words(size_t n)
 }
 
 // Sorts (keys, vals) by the low `bits` bits of the keys, stably. Ping-pongs
-// between the given buffers; returns which buffer holds the result (0 or 1).
-// vals0 may be null: the values are then the input positions.
+// between the given buffers (all four must be valid, n words each); returns
+// which pair holds the result (0 or 1). With positions_as_values the input
+// values are not read: value i is the input position i.
 cudaError_t radix_sort(uint32_t *keys0, uint32_t *keys1, uint32_t *vals0, uint32_t *vals1, size_t n,
                        int bits, uint32_t *hist, uint32_t *scan_tmp, cudaStream_t st, int *which,
-                       int *launches, bool keys_out)
+                       int *launches, bool keys_out, bool positions_as_values)
 {
     const uint32_t ntiles = (uint32_t)((n + kRsTile - 1) / kRsTile);
     int cur = 0;
-    const uint32_t *vin = vals0;
+    const uint32_t *vin = positions_as_values ? nullptr : vals0;
     for (int shift = 0; shift < bits; shift += 8)
     {
         uint32_t *kin = cur ? keys1 : keys0, *kout = cur ? keys0 : keys1;
@@ -407,7 +408,7 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         HC_CUDA(ctx, cudaMemcpyAsync(d_site0, hsite.data(), 8ull * n, cudaMemcpyHostToDevice, st));
         k_mass_keys<<<(n + 255) / 256, 256, 0, st>>>(d_m0, n, k0);
         int which = 0;
-        HC_CUDA(ctx, radix_sort(k0, k1, nullptr, v1, n, 32, hist, stmp, st, &which, &launches, false));
+        HC_CUDA(ctx, radix_sort(k0, k1, v0, v1, n, 32, hist, stmp, st, &which, &launches, false, true));
         // after an even number of passes the result is in (k0, v0)
         uint32_t *perm = which ? v1 : v0;
         k_gather_entries<<<(n + 255) / 256, 256, 0, st>>>(perm, n, d_m0, d_s0, d_site0, d_mod0,
@@ -434,7 +435,7 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         int bits = 1;
         while ((1ull << bits) < nb) bits++;
         int which = 0;
-        HC_CUDA(ctx, radix_sort(k0, k1, nullptr, v1, M, bits, hist, stmp, st, &which, &launches, true));
+        HC_CUDA(ctx, radix_sort(k0, k1, v0, v1, M, bits, hist, stmp, st, &which, &launches, true, true));
         uint32_t *skeys = which ? k1 : k0;
         uint32_t *svals = which ? v1 : v0;
         HC_CUDA(ctx, cudaMemcpyAsync(lh.d_iA, svals, 4 * M, cudaMemcpyDeviceToDevice, st));

@@ -108,6 +108,8 @@ struct hc_ctx
     std::string last_error;
     int last_launches = 0;
     bool lens_dirty = true;
+    bool profiling = false;
+    cudaEvent_t ev[5] = {};  // windows | search | wide | tailfit boundaries
 };
 
 namespace hc {

@@ -56,7 +56,7 @@ struct SearchArgs
     uint32_t *work;
     uint32_t tile;
     const uint32_t *only;   // optional list of spectra to process (wide pass)
-    uint32_t nonly;
+    const uint32_t *nonly_dev;  // its length, in device memory
 };
 
 __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t *__restrict__ a, uint32_t lo,
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(1024) k_search(SearchArgs a)
         if (tid == 0)
         {
             uint32_t w = atomicAdd(a.work, 1u);
-            T.spec = a.only ? (w < a.nonly ? a.only[w] : 0xFFFFFFFFu) : (w < a.nspec ? w : 0xFFFFFFFFu);
+            T.spec = a.only ? (w < *a.nonly_dev ? a.only[w] : 0xFFFFFFFFu) : (w < a.nspec ? w : 0xFFFFFFFFu);
         }
         for (int i = tid; i < HC_HIST_BINS; i += nthr) T.hist[i] = 0;
         __syncthreads();
@@ -748,6 +748,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 16, st));
 
     const uint64_t nw = (uint64_t)nspec * nlen;
+    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
     k_windows<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(ctx->d_lens, nlen, d_prec, d_dM, ctx->p.dM,
                                                             nspec, q.d_win);
     HC_CUDA(ctx, cudaGetLastError());
@@ -775,31 +776,29 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     const size_t smem = search_smem(a.tile, a.dF, false);
     HC_CUDA(ctx, cudaFuncSetAttribute(k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
+    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     k_search<false><<<grid, ctx->tuning.threads, smem, st>>>(a);
     HC_CUDA(ctx, cudaGetLastError());
 
-    // spectra whose packed scorecard could overflow: redo them wide
-    uint32_t nwide = 0;
-    HC_CUDA(ctx, cudaMemcpyAsync(&nwide, q.d_nwide, 4, cudaMemcpyDeviceToHost, st));
-    HC_CUDA(ctx, cudaStreamSynchronize(st));
-    int launches = 2;
-    if (nwide > 0)
-    {
-        SearchArgs b = a;
-        b.only = q.d_wide;
-        b.nonly = nwide;
-        b.work = q.d_work + 1;
-        b.tile = ctx->tuning.tile / 2;
-        const size_t smem2 = search_smem(b.tile, b.dF, true);
-        HC_CUDA(ctx, cudaFuncSetAttribute(k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-        k_search<true><<<grid, ctx->tuning.threads, smem2, st>>>(b);
-        HC_CUDA(ctx, cudaGetLastError());
-        launches++;
-    }
+    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
+    // spectra whose packed scorecard could overflow are redone wide; the
+    // list length is read on the device (no host synchronisation)
+    SearchArgs b = a;
+    b.only = q.d_wide;
+    b.nonly_dev = q.d_nwide;
+    b.work = q.d_work + 1;
+    b.tile = ctx->tuning.tile / 2;
+    const size_t smem2 = search_smem(b.tile, b.dF, true);
+    HC_CUDA(ctx, cudaFuncSetAttribute(k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+    k_search<true><<<grid, ctx->tuning.threads, smem2, st>>>(b);
+    HC_CUDA(ctx, cudaGetLastError());
+    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
                                                                             ctx->p.expect_max);
     HC_CUDA(ctx, cudaGetLastError());
-    ctx->last_launches = launches + 1;
+    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[4], st));
+    int launches = 4;
+    ctx->last_launches = launches;
     return HC_SUCCESS;
 }
 

@@ -129,6 +129,15 @@ class Index:
     def last_launch_count(self) -> int:
         return self.lib.hc_last_launch_count(self.ctx)
 
+    def set_profiling(self, on: bool = True):
+        self._check(self.lib.hc_ctx_set_profiling(self.ctx, int(on)), "hc_ctx_set_profiling")
+
+    def kernel_times(self) -> dict:
+        """Device ms of each query stage of the last query (profiling on)."""
+        t = [C.c_float() for _ in range(4)]
+        self._check(self.lib.hc_last_kernel_times(self.ctx, *[C.byref(x) for x in t]), "hc_last_kernel_times")
+        return dict(zip(("windows", "search", "wide", "tailfit"), (x.value for x in t)))
+
     def identity(self, res: np.ndarray):
         """(seqid, modnum, sites) of each top hit (-1 where none)."""
         n = res.shape[0]

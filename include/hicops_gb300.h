@@ -157,8 +157,19 @@ int hc_dslim_query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_
                           const uint32_t *d_intensity, const float *d_precurse,
                           const double *d_dM, uint32_t nspec, uint32_t npeaks,
                           hc_result *d_out, uint32_t *d_hist, void *stream);
+/* Host-side check of the postings-id decoding: counts x in [0, xmax) for
+ * which the multiply-shift quotient used on the device differs from x / d
+ * (0 expected; no device needed). */
+uint64_t hc_check_division(uint32_t d, uint32_t xmax);
 /* Kernel launches made by the last query call (for launch accounting). */
 int hc_last_launch_count(const hc_ctx *ctx);
+/* With profiling on, every query records CUDA events around its kernels on
+ * the query stream; hc_last_kernel_times waits for the last query and
+ * returns the device time of each stage in ms (window search, packed search,
+ * wide search, tail fit). */
+int hc_ctx_set_profiling(hc_ctx *ctx, int on);
+int hc_last_kernel_times(hc_ctx *ctx, float *ms_windows, float *ms_search, float *ms_wide,
+                         float *ms_tailfit);
 
 #ifdef __cplusplus
 }

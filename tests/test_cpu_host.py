@@ -1,0 +1,102 @@
+"""CPU tests of the library boundary and its host logic (no device compute)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from hicops_gb300 import _lib as L
+from hicops_gb300 import synthetic as S
+from hicops_gb300.params import gParams, parse_uparams
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.load()
+    with open(os.path.join(ROOT, "include", "hicops_gb300.h")) as f:
+        hdr = f.read()
+    decl = set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(hc_[a-z_0-9]+)\s*\(", hdr, re.M))
+    assert len(decl) >= 15
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert set(L.EXPORTED) <= decl
+    assert lib.hc_version() >= 10000
+
+
+def test_ctx_create_without_device_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    from hicops_gb300 import dslim
+    with pytest.raises(L.HcError) as e:
+        dslim.Index(S.SearchParams())
+    assert e.value.status == -3022
+
+
+def test_bad_params_rejected():
+    import ctypes as C
+    lib = L.load()
+    p = S.SearchParams()
+    p.max_len = 80
+    h = C.c_void_p()
+    assert lib.hc_ctx_create(0, C.byref(L.to_hc_params(p)), C.byref(h)) == -3002
+
+
+@pytest.mark.parametrize("maxz", [1, 2, 3, 4, 5])
+def test_division_constants_exact(maxz):
+    lib = L.load()
+    for Lp in range(2, 63):
+        d = 2 * maxz * (Lp - 1)
+        # exhaustive over the first 2^20 ids, plus the top of the 2^31 range
+        assert lib.hc_check_division(d, 1 << 20) == 0, d
+
+
+def _entries_c(p, L_, seqs):
+    import ctypes as C
+    lib = L.load()
+    cp = L.to_hc_params(p)
+    seqs = np.ascontiguousarray(seqs, np.uint8)
+    n = lib.hc_make_entries(C.byref(cp), L_, L.ptr(seqs), seqs.shape[0], None, 0)
+    out = np.zeros(n, L.ENTRY_DTYPE)
+    assert lib.hc_make_entries(C.byref(cp), L_, L.ptr(seqs), seqs.shape[0], L.ptr(out), n) == n
+    return out
+
+
+@pytest.mark.parametrize("mods", [[], [("M", 15.99, 2)], [("M", 15.99, 2), ("STY", 79.97, 1)]])
+def test_host_entries_match_oracle(mods):
+    p = S.SearchParams(maxz=3, vmods_per_pep=2 if mods else 0, mods=mods)
+    db = S.make_database(800, 31, p)
+    for L_ in (7, 15, 40):
+        a = _entries_c(p, L_, db[L_])
+        b = O.make_entries(db[L_], L_, p, sort=False)
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), L_
+
+
+def test_uparams_parser_quirks(tmp_path):
+    f = tmp_path / "uparams.txt"
+    f.write_text("\n".join(["/db/", "/ms2", "/ws", "8", "2", "7", "40", "3", "0.01", "500", "0.01", "100",
+                            "500", "5000", "10", "20", "4", "4", "100", "0.01", "2048", "cyclic", "1", "2",
+                            "M", "15.994915", "2"]) + "\n")
+    p = parse_uparams(str(f))
+    assert p.dF == 1 and p.scale == 100 and p.base_int == 100000 and p.min_int == 1000
+    assert p.spadmem == 2048 * 1024 * 1024 and p.mods == [("M", 15.994915, 2)] and p.vmods_per_pep == 2
+    assert p.mod_mass_scaled(0) == 1599
+
+
+def test_generator_is_seeded():
+    p = S.SearchParams(maxz=2)
+    a = S.make_database(300, 5, p)
+    b = S.make_database(300, 5, p)
+    assert all(np.array_equal(a[k], b[k]) for k in a)
+    qa = S.make_queries(a, 20, 6, p)
+    qb = S.make_queries(b, 20, 6, p)
+    assert np.array_equal(qa.moz, qb.moz) and np.array_equal(qa.intensity, qb.intensity)
+    # pickpeaks: at most QALEN peaks, ascending intensity, top = base_int
+    for s in range(qa.nspec):
+        i0, i1 = qa.idx[s], qa.idx[s + 1]
+        it = qa.intensity[i0:i1]
+        assert i1 - i0 <= 100 and np.all(np.diff(it.astype(np.int64)) >= 0)
+        if i1 > i0:
+            assert it[-1] == p.base_int and it.min() >= p.min_int
