@@ -31,7 +31,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "spectra/s & postings GB/s vs HBM peak: batched+learned vs plain GPU, same PSMs"
-WORKLOAD = "open-2m"
+WORKLOAD = os.environ.get("HC_WORKLOAD", "open-2m")
 CPU_SAMPLE = int(os.environ.get("HC_CPU_SAMPLE", "2000"))
 
 
@@ -250,7 +250,7 @@ def run_gpu(args, rank, world, dist):
     out = {"metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "peptides": 2000000, "entries": None, "postings": None,
+           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()), "entries": None, "postings": None,
                       "spectra_per_step": n, "peaks_per_spectrum": 100, "dF_bins": p.dF, "dM_da": p.dM,
                       "maxz": p.maxz, "mods": "M+15.99 <=2", "parallelism": f"replicas{world}",
                       "l2": "index (~2 GB postings) larger than L2; no flush", "form": "plain",
@@ -284,7 +284,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default=None, help="open-2m (default), open-200k, plain-20k, mixed-2m")
     args = ap.parse_args()
+    if args.workload:
+        global WORKLOAD
+        WORKLOAD = args.workload
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, dist)

@@ -315,6 +315,9 @@ def workload(name: str):
     if name == "open-2m":         # 2M peptides + M-ox (<=2), 100k spectra, dF 0.01, dM 500, z 1-3
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 2000000, 0xC10, 100000, 0xC11, {}
+    if name == "open-200k":       # open-2m's shape at 1/10 of the database, 5,000 spectra (profiling)
+        p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+        return p, 200000, 0xC12, 5000, 0xC13, {}
     if name == "mixed-2m":        # open-2m index, 200k spectra, 20-150 peaks, mixed windows
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 2000000, 0xC10, 200000, 0xC21, dict(
