@@ -119,11 +119,12 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     const uint32_t nlen = p->max_len - p->min_len + 1;
     ctx->lens.resize(nlen);
     for (uint32_t i = 0; i < nlen; i++) ctx->lens[i].L = p->min_len + i;
-    // default launch shape: one 512-thread CTA per SM, 16k-candidate tiles
+    // default launch shape: one 512-thread CTA per SM, 4 postings lists in
+    // flight per warp, the largest scorecard tile the shared memory holds
     ctx->tuning.threads = 512;
-    ctx->tuning.tile = 16384;
+    ctx->tuning.tile = max_tile(ctx, p->dF);
     ctx->tuning.ctas_per_sm = 1;
-    ctx->tuning.pairs_per_warp = 1;
+    ctx->tuning.pairs_per_warp = 4;
     *out = ctx;
     return HC_SUCCESS;
 }
@@ -154,8 +155,12 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
 {
     if (!ctx || !t) return HC_ERR_INVLD_PTR;
     if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < 256 || (t->tile & 1) ||
-        t->ctas_per_sm < 1 || t->ctas_per_sm > 8)
+        t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
+        (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8))
         return set_error(ctx, HC_ERR_INVLD_PARAM, "bad tuning");
+    if (search_smem(t->tile, ctx->p.dF, false) * t->ctas_per_sm > ctx->smem_optin + 1024 * (t->ctas_per_sm - 1) ||
+        search_smem(t->tile, ctx->p.dF, false) > ctx->smem_optin)
+        return set_error(ctx, HC_ERR_INVLD_PARAM, "tile does not fit in shared memory");
     ctx->tuning = *t;
     return HC_SUCCESS;
 }
@@ -255,7 +260,7 @@ int hc_dslim_load(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep, c
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_modnum, 4ull * n + 4));
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_sites, 8ull * n + 8));
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_bA, 4ull * (nb + 1)));
-    HC_CUDA(ctx, cudaMalloc((void **)&lh->d_iA, 4 * M + 4));
+    HC_CUDA(ctx, cudaMalloc((void **)&lh->d_iA, 4 * (M + kIaPad)));
     HC_CUDA(ctx, cudaMemcpy(lh->d_mass, m.data(), 4ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_seqid, s.data(), 4ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_modnum, mo.data(), 4ull * n, cudaMemcpyHostToDevice));

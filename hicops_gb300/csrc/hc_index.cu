@@ -381,7 +381,7 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
     HC_CUDA(ctx, dalloc(&lh.d_sites, n));
     HC_CUDA(ctx, dalloc(&lh.d_modnum, n));
     HC_CUDA(ctx, dalloc(&lh.d_bA, (size_t)nb + 1));
-    HC_CUDA(ctx, dalloc(&lh.d_iA, M));
+    HC_CUDA(ctx, dalloc(&lh.d_iA, M + kIaPad));  // padded: the query reads 16-byte groups
 
     // scratch: keys/vals ping-pong, radix histograms, scan temp
     const size_t items = M > n ? M : n;

@@ -15,6 +15,7 @@ namespace hc {
 constexpr int kMaxZ = 8;           // fragment charges handled (the reference clamps maxz <= 5)
 constexpr int kLgTable = 256;      // lgfact entries kept on the device (flagged past 80)
 constexpr int kRefMaxShp = 81;     // MAX_SHDPEAKS + 1 (utils.h:110)
+constexpr size_t kIaPad = 128;     // postings arrays are padded: the query reads aligned 16-byte groups
 
 // One peptide length's device-resident index. All arrays are device pointers.
 struct LenDev
@@ -125,6 +126,8 @@ void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
 
 // hc_query.cu
+uint32_t max_tile(const hc_ctx *ctx, uint32_t dF);
+size_t search_smem(uint32_t tile, uint32_t dF, bool wide);
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
                  hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);

@@ -35,7 +35,7 @@
 namespace hc {
 namespace {
 
-constexpr int kQcap = 2048;         // qualifying-candidate list per tile
+constexpr int kQcap = 3072;         // qualifying-candidate list per tile
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
 constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
@@ -97,8 +97,9 @@ struct Card;
 template <>
 struct Card<false>
 {
-    // [bc:8 | yc:8 | ibc:24 | iyc:24]; counts are kept below 128 (checked per
-    // posting), so with intensities < 2^17 the sums stay below 2^24.
+    // [shp:8 | bc:8 | ibc:24 | iyc:24] with shp = bc + yc; shp is kept below
+    // 128 (checked per posting), so with intensities < 2^17 the sums stay
+    // below 2^24 and no field can carry into the next.
     using word = unsigned long long;
     static constexpr int kWords = 1;
 };
@@ -124,6 +125,8 @@ struct SmemTail
     uint32_t overflow;
     uint32_t spec;
     uint32_t nv;
+    uint32_t pnext;            // next postings list to hand out
+    uint32_t pad1;
     unsigned long long bytes;
     float lgf[kLgTable];
 };
@@ -147,8 +150,67 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     return o;
 }
 
+__device__ __forceinline__ float approx_h(const float *lgf, uint32_t bc, uint32_t yc, uint64_t ib, uint64_t iy)
+{
+    return ((lgf[bc] + lgf[yc]) + log10f((float)(1 + ib))) + log10f((float)(1 + iy)) - 6.0f;
+}
+
 template <bool WIDE>
-__global__ void __launch_bounds__(1024) k_search(SearchArgs a)
+__device__ __forceinline__ void decode(const unsigned long long *card, uint32_t loc, uint32_t &bc, uint32_t &yc,
+                                       uint32_t &shp, uint64_t &ib, uint64_t &iy)
+{
+    if constexpr (!WIDE)
+    {
+        const unsigned long long wd = card[loc];
+        bc = (uint32_t)(wd >> 48) & 0xFF;
+        yc = (uint32_t)(wd >> 56) - bc;
+        ib = (wd >> 24) & 0xFFFFFF;
+        iy = wd & 0xFFFFFF;
+    }
+    else
+    {
+        const unsigned long long wb = card[2 * loc], wy = card[2 * loc + 1];
+        bc = (uint32_t)(wb >> 40);
+        yc = (uint32_t)(wy >> 40);
+        ib = wb & 0xFFFFFFFFFFull;
+        iy = wy & 0xFFFFFFFFFFull;
+    }
+    // the reference reads bc/yc through short/ushort (dslim_query.cpp:684-686)
+    shp = (uint32_t)(uint16_t)(bc + yc);
+}
+
+// Hyperscore of one candidate: returns false unless h > 0; h is the float
+// estimate (or the reference's value where the estimate's bound leaves the
+// sign or the histogram bin undecided), bin its histogram bin.
+template <bool WIDE>
+__device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const float *lgf, uint32_t bc, uint32_t yc,
+                                      uint64_t ib, uint64_t iy, float &h, int &bin)
+{
+    if (!WIDE)
+    {
+        const float ha = approx_h(lgf, bc, yc, ib, iy);
+        const float t = ha * 10.0f + 0.5f;
+        const float fr = t - floorf(t);
+        if (!(fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin))
+        {
+            h = ha;
+            bin = (int)floorf(t);
+            return ha > 0.0f;
+        }
+    }
+    const float hf = exact_h(qc, bc, yc, ib, iy);
+    h = hf;
+    bin = hist_bin(hf);
+    return hf > 0.0f;
+}
+
+__device__ __forceinline__ uint4 ldg4(const uint32_t *p)
+{
+    return __ldg(reinterpret_cast<const uint4 *>(p));
+}
+
+template <bool WIDE, int G>
+__global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
 {
     using W = typename Card<WIDE>::word;
     constexpr int NW = Card<WIDE>::kWords;
@@ -226,157 +288,189 @@ __global__ void __launch_bounds__(1024) k_search(SearchArgs a)
             if (w.x > w.y) continue;
             const LenDev d = a.lens[l];
             const uint32_t lo_id = (uint32_t)w.x * d.speclen;
-            const uint32_t hi_id = (uint32_t)(w.y + 1) * d.speclen;
-            uint32_t my_bytes = 0;
+            // A window covering a quarter of the length or more is entered at
+            // each bucket's start: postings below the window are read and
+            // dropped by the tile bound below (cheaper than a dependent
+            // binary search per bucket). Narrower windows search their start.
+            const bool skip_in_stream = 4ull * (uint64_t)(w.y - w.x + 1) >= (uint64_t)d.n;
             for (uint32_t pr = tid; pr < np; pr += nthr)
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 const uint32_t bin = pmoz[k] - a.dF + j;
                 const uint32_t st = __ldg(d.bA + bin), en = __ldg(d.bA + bin + 1);
-                uint32_t c = st, e = st;
-                if (en > st)
-                {
-                    c = (__ldg(d.iA + st) >= lo_id) ? st : lower_bound_g(d.iA, st + 1, en, lo_id);
-                    e = (__ldg(d.iA + en - 1) < hi_id) ? en : lower_bound_g(d.iA, c, en, hi_id);
-                }
+                uint32_t c = st;
+                if (!skip_in_stream && en > st && __ldg(d.iA + st) < lo_id)
+                    c = lower_bound_g(d.iA, st + 1, en, lo_id);
                 pcur[pr] = c;
-                pend[pr] = e;
-                my_bytes += e - c;
+                pend[pr] = en;
             }
-            if (my_bytes) atomicAdd(&T.bytes, 4ull * my_bytes);
-            if (tid == 0) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);
+            if (tid == 0)
+            {
+                atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);
+                T.pnext = 0;
+            }
+            uint32_t my_inwin = 0;
             __syncthreads();
 
             for (uint32_t c0 = (uint32_t)w.x; c0 <= (uint32_t)w.y; c0 += tile)
             {
                 const uint32_t c1 = min(c0 + tile, (uint32_t)w.y + 1);
+                const uint32_t ntile = c1 - c0;
                 const uint32_t tile_hi = c1 * d.speclen;
                 // ---- stream postings into the scorecard tile ----
-                for (uint32_t pr = warp; pr < np; pr += nwarps)
+                // A warp keeps G (peak, bin) lists in flight; each step loads
+                // 128 ids per list with one 16-byte load per lane (the list is
+                // entered at its 16-byte-aligned position; ids before the
+                // cursor or past the list end are masked).
+                // lists are handed out G at a time to whichever warp is free
+                for (;;)
                 {
-                    uint32_t cur = pcur[pr];
-                    const uint32_t end = pend[pr];
-                    const uint32_t intn = pint[pr / nbin];
-                    while (cur < end)
+                    uint32_t base = 0;
+                    if (lane == 0) base = atomicAdd(&T.pnext, (uint32_t)G);
+                    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                    if (base >= np) break;
+                    uint32_t cur[G], end[G], intn[G];
+                    bool live[G];
+#pragma unroll
+                    for (int g = 0; g < G; g++)
                     {
-                        const uint32_t i = cur + lane;
-                        const uint32_t id = (i < end) ? __ldg(d.iA + i) : 0xFFFFFFFFu;
-                        const bool take = id < tile_hi;
-                        const uint32_t m = __ballot_sync(0xFFFFFFFFu, take);
-                        if (take)
+                        const uint32_t pr = base + g;
+                        live[g] = pr < np;
+                        cur[g] = live[g] ? pcur[pr] : 0u;
+                        end[g] = live[g] ? pend[pr] : 0u;
+                        intn[g] = live[g] ? pint[pr / nbin] : 0u;
+                        live[g] = live[g] && cur[g] < end[g];
+                    }
+                    for (;;)
+                    {
+                        bool any = false;
+#pragma unroll
+                        for (int g = 0; g < G; g++) any |= live[g];
+                        if (!any) break;
+                        uint4 v[G];
+                        uint32_t a0[G];
+#pragma unroll
+                        for (int g = 0; g < G; g++)
                         {
-                            const uint32_t ppid = __umulhi(id, d.magic) >> d.msh;
-                            const uint32_t loc = ppid - c0;
-                            const bool isY = (id - ppid * d.speclen) >= d.half;
-                            if (loc >= c1 - c0)
-                            {   // only an unsorted bucket can land here; never index past the tile
-                                T.overflow = 1;
-                            }
-                            else if constexpr (!WIDE)
+                            a0[g] = cur[g] & ~3u;
+                            const uint32_t p = a0[g] + 4u * lane;
+                            v[g] = (live[g] && p < end[g]) ? ldg4(d.iA + p)
+                                                           : make_uint4(~0u, ~0u, ~0u, ~0u);
+                        }
+#pragma unroll
+                        for (int g = 0; g < G; g++)
+                        {
+                            if (!live[g]) continue;
+                            const uint32_t ids[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
+                            const uint32_t p0 = a0[g] + 4u * lane;
+                            uint32_t cnt = 0;
+#pragma unroll
+                            for (int j = 0; j < 4; j++)
                             {
-                                const W add = isY ? ((1ull << 48) | (W)intn)
-                                                  : ((1ull << 56) | ((W)intn << 24));
-                                const W old = atomicAdd(&card[loc], add);
-                                const uint32_t cb = (uint32_t)(old >> 56), cy = (uint32_t)(old >> 48) & 0xFF;
-                                if ((isY ? cy : cb) >= 127u) T.overflow = 1;
-                                if (cb + cy + 1 == a.thr)
+                                const uint32_t p = p0 + j, id = ids[j];
+                                if (p >= cur[g] && p < end[g] && id < tile_hi)
                                 {
-                                    const uint32_t qi = atomicAdd(&T.qcount, 1u);
-                                    if (qi < kQcap) qual[qi] = loc;
+                                    cnt++;
+                                    const uint32_t ppid = __umulhi(id, d.magic) >> d.msh;
+                                    const uint32_t loc = ppid - c0;
+                                    if (loc < ntile)  // below the window (or tile): not a hit here
+                                    {
+                                        my_inwin++;
+                                        const bool isY = (id - ppid * d.speclen) >= d.half;
+                                        if constexpr (!WIDE)
+                                        {
+                                            // word = [shp:8 | bc:8 | ibc:24 | iyc:24]
+                                            const W add = isY ? ((1ull << 56) | (W)intn[g])
+                                                              : ((1ull << 56) | (1ull << 48) | ((W)intn[g] << 24));
+                                            const W old = atomicAdd(&card[loc], add);
+                                            const uint32_t sh8 = (uint32_t)(old >> 56);
+                                            if (sh8 >= 127u) T.overflow = 1;
+                                            if (sh8 + 1 == a.thr)
+                                            {
+                                                const uint32_t qi = atomicAdd(&T.qcount, 1u);
+                                                if (qi < kQcap) qual[qi] = loc;
+                                            }
+                                        }
+                                        else
+                                        {
+                                            atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)intn[g]);
+                                        }
+                                    }
                                 }
                             }
-                            else
-                            {
-                                // candidates are found by scanning the tile below
-                                atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)intn);
-                            }
+                            const uint32_t consumed = __reduce_add_sync(0xFFFFFFFFu, cnt);
+                            const uint32_t chunk_hi = min(end[g], a0[g] + 128u);
+                            const bool whole = consumed == chunk_hi - cur[g];
+                            cur[g] += consumed;
+                            live[g] = whole && cur[g] < end[g];
                         }
-                        const uint32_t cnt = __popc(m);
-                        cur += cnt;
-                        if (cnt < 32) break;
                     }
-                    if (lane == 0) pcur[pr] = cur;
+                    if (lane == 0)
+                    {
+#pragma unroll
+                        for (int g = 0; g < G; g++)
+                        {
+                            const uint32_t pr = base + g;
+                            if (pr < np) pcur[pr] = cur[g];
+                        }
+                    }
                 }
                 __syncthreads();
                 // ---- score the candidates that reached min_shp ----
+                // pass 1: hyperscore (float, exact where the bound leaves the
+                // sign or the bin open), cpsms, histogram, tile maximum
                 const uint32_t qn = T.qcount;
                 const bool scan_all = WIDE || qn > (uint32_t)kQcap || a.thr > 250;
                 const uint32_t nscore = scan_all ? (c1 - c0) : qn;
+                float my_max = 0.0f;
+                uint32_t my_cps = 0, my_fl = 0;
                 for (uint32_t i = tid; i < nscore; i += nthr)
                 {
                     const uint32_t loc = scan_all ? i : qual[i];
-                    uint32_t bc, yc;
+                    uint32_t bc, yc, shp;
                     uint64_t ib, iy;
-                    if constexpr (!WIDE)
-                    {
-                        const W wd = card[loc];
-                        bc = (uint32_t)(wd >> 56);
-                        yc = (uint32_t)(wd >> 48) & 0xFF;
-                        ib = (wd >> 24) & 0xFFFFFF;
-                        iy = wd & 0xFFFFFF;
-                    }
-                    else
-                    {
-                        const W wb = card[2 * loc], wy = card[2 * loc + 1];
-                        bc = (uint32_t)(wb >> 40);
-                        yc = (uint32_t)(wy >> 40);
-                        ib = wb & 0xFFFFFFFFFFull;
-                        iy = wy & 0xFFFFFFFFFFull;
-                    }
-                    // reference reads bc/yc through short/ushort (dslim_query.cpp:684-686)
-                    const uint32_t shp = (uint32_t)(uint16_t)(bc + yc);
+                    decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
                     if (shp < a.min_shp || shp == 0) continue;
-                    float hf;
-                    bool pos;
+                    float h;
                     int bin;
-                    bool exact = WIDE;
-                    float ha = 0.0f;
-                    if (!exact)
-                    {
-                        ha = ((T.lgf[bc] + T.lgf[yc]) + log10f((float)(1 + ib))) + log10f((float)(1 + iy)) - 6.0f;
-                        const float t = ha * 10.0f + 0.5f;
-                        const float fr = t - floorf(t);
-                        if (fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin)
-                            exact = true;
-                        else
-                        {
-                            pos = ha > 0.0f;
-                            bin = (int)floorf(t);
-                            hf = ha;
-                        }
-                    }
-                    if (exact)
-                    {
-                        hf = exact_h(a.qc, bc, yc, ib, iy);
-                        pos = hf > 0.0f;
-                        bin = hist_bin(hf);
-                        ha = hf;
-                    }
-                    if (!pos) continue;
-                    atomicAdd(&T.cpsms, 1u);
-                    uint32_t fl = 0;
-                    if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) fl |= HC_FLAG_LGFACT_OOB;
-                    if (bin >= HC_HIST_BINS || bin < 0) { fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
-                    if (fl) atomicOr(&T.flags, fl);
+                    if (!score<WIDE>(a.qc, T.lgf, bc, yc, ib, iy, h, bin)) continue;
+                    my_cps++;
+                    if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
+                    if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
                     atomicAdd(&T.hist[bin], 1u);
-                    // top-hit tracking: exact value for anything near the running max
-                    const uint32_t hb = __float_as_uint(ha);
-                    const uint32_t oldmax = atomicMax(&T.maxbits, hb);
-                    const float runmax = fmaxf(__uint_as_float(oldmax), ha);
-                    if (ha >= runmax - kNear)
-                    {
-                        const float he = WIDE ? hf : exact_h(a.qc, bc, yc, ib, iy);
-                        const uint32_t psid = c0 + loc;
-                        const uint32_t tie = (l << 24) | (psid & 0xFFFFFF);
-                        const unsigned long long key =
-                            ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
-                        if (key > my_best)
+                    my_max = fmaxf(my_max, h);
+                }
+                if (my_cps) atomicAdd(&T.cpsms, my_cps);
+                if (my_fl) atomicOr(&T.flags, my_fl);
+                if (my_max > 0.0f) atomicMax(&T.maxbits, __float_as_uint(my_max));
+                __syncthreads();
+                // pass 2: the reference's double hyperscore for every candidate
+                // that can still be the top hit (within kNear of the maximum so far)
+                {
+                    const float runmax = __uint_as_float(T.maxbits);
+                    if (runmax > 0.0f)
+                        for (uint32_t i = tid; i < nscore; i += nthr)
                         {
-                            my_best = key;
-                            my_shp = shp;
+                            const uint32_t loc = scan_all ? i : qual[i];
+                            uint32_t bc, yc, shp;
+                            uint64_t ib, iy;
+                            decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
+                            if (shp < a.min_shp || shp == 0) continue;
+                            const float ha = WIDE ? exact_h(a.qc, bc, yc, ib, iy) : approx_h(T.lgf, bc, yc, ib, iy);
+                            if (ha < runmax - kNear) continue;
+                            const float he = WIDE ? ha : exact_h(a.qc, bc, yc, ib, iy);
+                            if (!(he > 0.0f)) continue;
+                            const uint32_t psid = c0 + loc;
+                            const uint32_t tie = (l << 24) | (psid & 0xFFFFFF);
+                            const unsigned long long key =
+                                ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
+                            if (key > my_best)
+                            {
+                                my_best = key;
+                                my_shp = shp;
+                            }
+                            atomicMax(&T.best, key);
                         }
-                        atomicMax(&T.best, key);
-                    }
                 }
                 __syncthreads();
                 if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
@@ -387,9 +481,14 @@ __global__ void __launch_bounds__(1024) k_search(SearchArgs a)
                     const uint32_t n4 = (nw + 1) / 2;
                     for (uint32_t i = tid; i < n4; i += nthr) c4[i] = make_uint4(0, 0, 0, 0);
                 }
-                if (tid == 0) T.qcount = 0;
+                if (tid == 0)
+                {
+                    T.qcount = 0;
+                    T.pnext = 0;
+                }
                 __syncthreads();
             }
+            if (my_inwin) atomicAdd(&T.bytes, 4ull * my_inwin);
         }
         // ---- write the spectrum's results ----
         if (!WIDE && T.overflow)
@@ -684,7 +783,42 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
     out[s] = r;
 }
 
+}  // namespace
+
 size_t search_smem(uint32_t tile, uint32_t dF, bool wide) { return smem_layout(tile, dF, wide).total; }
+
+uint32_t max_tile(const hc_ctx *ctx, uint32_t dF)
+{
+    const size_t extra = smem_layout(0, dF, false).total;
+    const size_t room = ctx->smem_optin > extra ? ctx->smem_optin - extra : 0;
+    uint32_t t = (uint32_t)(room / 8) & ~511u;
+    return t < 512 ? 512 : t;
+}
+
+namespace {
+
+template <bool WIDE, int G>
+int launch_g(hc_ctx *ctx, const SearchArgs &a, int grid, uint32_t threads, size_t smem, cudaStream_t st)
+{
+    if (G >= 4 && threads > 512) threads = 512;
+    HC_CUDA(ctx, cudaFuncSetAttribute(k_search<WIDE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_search<WIDE, G><<<grid, threads, smem, st>>>(a);
+    HC_CUDA(ctx, cudaGetLastError());
+    return HC_SUCCESS;
+}
+
+template <bool WIDE>
+int launch_search(hc_ctx *ctx, const SearchArgs &a, int grid, uint32_t threads, size_t smem, uint32_t g,
+                  cudaStream_t st)
+{
+    switch (g)
+    {
+    case 1: return launch_g<WIDE, 1>(ctx, a, grid, threads, smem, st);
+    case 2: return launch_g<WIDE, 2>(ctx, a, grid, threads, smem, st);
+    case 8: return launch_g<WIDE, 8>(ctx, a, grid, threads, smem, st);
+    default: return launch_g<WIDE, 4>(ctx, a, grid, threads, smem, st);
+    }
+}
 
 }  // namespace
 
@@ -774,12 +908,10 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.work = q.d_work;
     a.tile = ctx->tuning.tile;
     const size_t smem = search_smem(a.tile, a.dF, false);
-    HC_CUDA(ctx, cudaFuncSetAttribute(k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
-    k_search<false><<<grid, ctx->tuning.threads, smem, st>>>(a);
-    HC_CUDA(ctx, cudaGetLastError());
-
+    int rc2 = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
+    if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
     // spectra whose packed scorecard could overflow are redone wide; the
     // list length is read on the device (no host synchronisation)
@@ -789,9 +921,8 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     b.work = q.d_work + 1;
     b.tile = ctx->tuning.tile / 2;
     const size_t smem2 = search_smem(b.tile, b.dF, true);
-    HC_CUDA(ctx, cudaFuncSetAttribute(k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-    k_search<true><<<grid, ctx->tuning.threads, smem2, st>>>(b);
-    HC_CUDA(ctx, cudaGetLastError());
+    rc2 = launch_search<true>(ctx, b, grid, ctx->tuning.threads, smem2, 2, st);
+    if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
                                                                             ctx->p.expect_max);
