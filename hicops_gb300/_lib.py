@@ -46,7 +46,7 @@ class HcParams(C.Structure):
 
 class HcTuning(C.Structure):
     _fields_ = [("threads", C.c_uint32), ("tile", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("pairs_per_warp", C.c_uint32)]
+                ("pairs_per_warp", C.c_uint32), ("schedule", C.c_uint32)]
 
 
 def to_hc_params(p) -> HcParams:
@@ -89,6 +89,11 @@ _SIGS = [
                                         C.c_void_p]),
     ("hc_last_launch_count", C.c_int, [C.c_void_p]),
     ("hc_check_division", C.c_uint64, [C.c_uint32, C.c_uint32]),
+    ("hc_dslim_query_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    ("hc_tune", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                          C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
     ("hc_ctx_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("hc_last_kernel_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float)]),

@@ -125,6 +125,7 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     ctx->tuning.tile = max_tile(ctx, p->dF);
     ctx->tuning.ctas_per_sm = 1;
     ctx->tuning.pairs_per_warp = 4;
+    ctx->tuning.schedule = 0;
     *out = ctx;
     return HC_SUCCESS;
 }
@@ -140,10 +141,14 @@ int hc_ctx_destroy(hc_ctx *ctx)
     cudaFree(ctx->qs.d_win);
     cudaFree(ctx->qs.d_wide);
     cudaFree(ctx->qs.d_work);
+    cudaFree(ctx->qs.d_order);
+    cudaFree(ctx->qs.d_fitstart);
     cudaFree(ctx->qs.d_in);
     cudaFree(ctx->qs.d_outbuf);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HC_SUCCESS;
@@ -156,7 +161,8 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
     if (!ctx || !t) return HC_ERR_INVLD_PTR;
     if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < 256 || (t->tile & 1) ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
-        (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8))
+        (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8) ||
+        t->schedule > 2)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "bad tuning");
     if (search_smem(t->tile, ctx->p.dF, false) * t->ctas_per_sm > ctx->smem_optin + 1024 * (t->ctas_per_sm - 1) ||
         search_smem(t->tile, ctx->p.dF, false) > ctx->smem_optin)

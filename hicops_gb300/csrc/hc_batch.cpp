@@ -1,0 +1,143 @@
+// Batched search support: CUDA-graph replay of the whole query pipeline and
+// the autotuner that picks the search launch shape (block size, scorecard
+// tile, postings lists in flight per warp, resident CTAs, schedule).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "hc_internal.h"
+
+namespace hc {
+
+static bool same_key(const GraphKey &a, const GraphKey &b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+
+}  // namespace hc
+
+using namespace hc;
+
+extern "C" {
+
+int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
+                         const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                         hc_result *d_out, uint32_t *d_hist, void *stream)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    if (nspec && (!d_idx || !d_moz || !d_intensity || !d_precurse || !d_out || !d_hist))
+        return set_error(ctx, HC_ERR_INVLD_PTR, "null device buffer");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    GraphKey key{};
+    key.idx = d_idx;
+    key.moz = d_moz;
+    key.inten = d_intensity;
+    key.prec = d_precurse;
+    key.dM = d_dM;
+    key.out = d_out;
+    key.hist = d_hist;
+    key.nspec = nspec;
+    key.npeaks = npeaks;
+    key.tuning = ctx->tuning;
+    if (!ctx->graph_exec || !same_key(key, ctx->graph_key))
+    {
+        if (ctx->graph_exec)
+        {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+        }
+        // everything that allocates or copies synchronously happens before capture
+        int rc = prepare_query(ctx, nspec);
+        if (rc) return rc;
+        if (!ctx->cap_stream) HC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        const bool prof = ctx->profiling;
+        ctx->profiling = false;
+        HC_CUDA(ctx, cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
+        rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist,
+                          ctx->cap_stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
+        ctx->profiling = prof;
+        if (rc) return rc;
+        HC_CUDA(ctx, e);
+        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        HC_CUDA(ctx, e);
+        ctx->graph_key = key;
+        ctx->graph_launches = ctx->last_launches;
+    }
+    HC_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, st));
+    ctx->last_launches = ctx->graph_launches;
+    return HC_SUCCESS;
+}
+
+int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
+            const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks, hc_result *d_out,
+            uint32_t *d_hist, hc_tuning *best, float *best_ms)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    if (nspec == 0) return set_error(ctx, HC_ERR_NOT_ENOUGH_DATA, "empty tuning sample");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    const hc_tuning saved = ctx->tuning;
+    const uint32_t full = max_tile(ctx, ctx->p.dF);
+    std::vector<hc_tuning> cand;
+    for (uint32_t sched : {0u, 2u})
+        for (uint32_t cps : {1u, 2u})
+            for (uint32_t thr : {256u, 512u, 1024u})
+                for (uint32_t g : {2u, 4u, 8u})
+                {
+                    if (g >= 4 && thr > 512) continue;
+                    hc_tuning t{};
+                    t.threads = thr;
+                    t.pairs_per_warp = g;
+                    t.ctas_per_sm = cps;
+                    t.schedule = sched;
+                    // two resident CTAs share the SM's shared memory
+                    t.tile = cps == 1 ? full : (max_tile_for(ctx, ctx->p.dF, cps));
+                    if (t.tile < 1024) continue;
+                    cand.push_back(t);
+                }
+    cudaEvent_t e0, e1;
+    HC_CUDA(ctx, cudaEventCreate(&e0));
+    HC_CUDA(ctx, cudaEventCreate(&e1));
+    float best_t = 1e30f;
+    hc_tuning best_c = saved;
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;
+    int rc = HC_SUCCESS;
+    for (const hc_tuning &t : cand)
+    {
+        if (hc_ctx_set_tuning(ctx, &t) != HC_SUCCESS) continue;
+        rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist, st);
+        if (rc) break;
+        float ms[2];
+        for (int r = 0; r < 2 && !rc; r++)
+        {
+            cudaEventRecord(e0, st);
+            rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms[r], e0, e1);
+        }
+        if (rc) break;
+        const float m = std::min(ms[0], ms[1]);
+        if (m < best_t)
+        {
+            best_t = m;
+            best_c = t;
+        }
+    }
+    ctx->profiling = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc)
+    {
+        ctx->tuning = saved;
+        return rc;
+    }
+    ctx->tuning = best_c;
+    if (best) *best = best_c;
+    if (best_ms) *best_ms = best_t;
+    return HC_SUCCESS;
+}
+
+}  // extern "C"

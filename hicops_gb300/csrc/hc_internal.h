@@ -74,13 +74,24 @@ struct QueryScratch
     int2 *d_win = nullptr;        // nspec * nlen windows [minl, maxl]
     uint32_t *d_wide = nullptr;   // spectra that overflowed the packed scorecard
     uint32_t *d_nwide = nullptr;
-    uint32_t *d_work = nullptr;   // work-stealing counter
-    size_t win_cap = 0, wide_cap = 0;
+    uint32_t *d_work = nullptr;   // work counters | cost-class counts | cursors
+    uint32_t *d_order = nullptr;  // longest-first order | cost classes
+    int32_t *d_fitstart = nullptr;  // first regression bin of each spectrum's tail fit (-1: none)
+    size_t fit_cap = 0;
+    size_t win_cap = 0, wide_cap = 0, order_cap = 0;
     // host-path staging
     void *d_in = nullptr;
     size_t in_cap = 0;
     void *d_outbuf = nullptr;
     size_t out_cap = 0;
+};
+
+// What a captured query graph was recorded with; a call that differs re-captures.
+struct GraphKey
+{
+    const void *idx, *moz, *inten, *prec, *dM, *out, *hist;
+    uint32_t nspec, npeaks;
+    hc_tuning tuning;
 };
 
 struct Launch
@@ -111,6 +122,10 @@ struct hc_ctx
     bool lens_dirty = true;
     bool profiling = false;
     cudaEvent_t ev[5] = {};  // windows | search | wide | tailfit boundaries
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    hc::GraphKey graph_key{};
+    int graph_launches = 0;
 };
 
 namespace hc {
@@ -127,6 +142,8 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
 
 // hc_query.cu
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF);
+uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm);
+int prepare_query(hc_ctx *ctx, uint32_t nspec);
 size_t search_smem(uint32_t tile, uint32_t dF, bool wide);
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,

@@ -57,6 +57,8 @@ struct SearchArgs
     uint32_t tile;
     const uint32_t *only;   // optional list of spectra to process (wide pass)
     const uint32_t *nonly_dev;  // its length, in device memory
+    const uint32_t *order;  // optional processing order (longest first)
+    uint32_t persistent;    // 1: CTAs loop over a work counter; 0: one spectrum per CTA
 };
 
 __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t *__restrict__ a, uint32_t lo,
@@ -227,18 +229,21 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
 
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    const int lane = tid & 31;
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
     for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
 
-    for (;;)
+    for (uint32_t iter = 0;; iter++)
     {
         __syncthreads();
         if (tid == 0)
         {
-            uint32_t w = atomicAdd(a.work, 1u);
-            T.spec = a.only ? (w < *a.nonly_dev ? a.only[w] : 0xFFFFFFFFu) : (w < a.nspec ? w : 0xFFFFFFFFu);
+            const uint32_t w = a.persistent ? atomicAdd(a.work, 1u) : (iter == 0 ? blockIdx.x : 0xFFFFFFFFu);
+            uint32_t sp = 0xFFFFFFFFu;
+            if (a.only) sp = w < *a.nonly_dev ? a.only[w] : 0xFFFFFFFFu;
+            else if (w < a.nspec) sp = a.order ? a.order[w] : w;
+            T.spec = sp;
         }
         for (int i = tid; i < HC_HIST_BINS; i += nthr) T.hist[i] = 0;
         __syncthreads();
@@ -490,6 +495,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
             }
             if (my_inwin) atomicAdd(&T.bytes, 4ull * my_inwin);
         }
+        __syncthreads();  // every thread's byte count is in before thread 0 reads it
         // ---- write the spectrum's results ----
         if (!WIDE && T.overflow)
         {
@@ -620,7 +626,7 @@ constexpr int kTfWarps = 4;
 __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict__ out,
                                                           const uint32_t *__restrict__ hist,
                                                           uint32_t nspec, uint32_t min_cpsm,
-                                                          double expect_max)
+                                                          double expect_max, int32_t *__restrict__ fitstart)
 {
     __shared__ double sxs[kTfWarps][HC_HIST_BINS + 2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -633,9 +639,14 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
     r.reported = 0;
     if (r.cpsms < min_cpsm || r.cpsms == 0)
     {
-        if (lane == 0) out[s] = r;
+        if (lane == 0)
+        {
+            out[s] = r;
+            fitstart[s] = -1;
+        }
         return;
     }
+    int fit_first = -1;  // first regression bin (the learned tail's third target)
     const uint32_t *yy = hist + (size_t)s * HC_HIST_BINS;
     const int hyp = hist_bin(r.hyperscore);  // maxhypscore (dslim_query.cpp:778)
     const int cps = (int)r.cpsms;
@@ -735,6 +746,7 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
             if (mark >= mark2) mark = mark2 - 1;
         }
         if (mark < 0) fl |= HC_FLAG_TAILFIT_OOB;  // reads element -1 (sx[0] = +0.0)
+        fit_first = stt1 + mark;
         const int m = mark2 - mark + 1;
         const double *y = sx + 1 + mark;
         // LinearFit (expeRT.cpp:1297-1345) on lane 0, in the reference's order
@@ -767,6 +779,7 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
         }
     }
     if (lane != 0) return;
+    fitstart[s] = fit_first;
     r.flags |= fl;
     r.mu = x86_d2i(__dmul_rn(mu_t, 1e6));
     r.beta = x86_d2i(__dmul_rn(beta_t, 1e6));
@@ -783,9 +796,52 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
     out[s] = r;
 }
 
+// ---- longest-first order for the batched schedule --------------------------
+// cost class of a spectrum = bit length of its total window size (candidates)
+constexpr int kCostClasses = 64;
+
+__global__ void k_cost(const int2 *__restrict__ win, uint32_t nspec, uint32_t nlen, uint32_t *__restrict__ cls,
+                       uint32_t *__restrict__ cnt)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nspec) return;
+    unsigned long long c = 0;
+    for (uint32_t l = 0; l < nlen; l++)
+    {
+        const int2 w = win[(size_t)s * nlen + l];
+        if (w.y >= w.x) c += (unsigned long long)(w.y - w.x + 1);
+    }
+    const uint32_t k = c ? 64u - (uint32_t)__clzll(c) : 0u;
+    cls[s] = k;
+    atomicAdd(&cnt[k], 1u);
+}
+
+__global__ void k_order(const uint32_t *__restrict__ cls, uint32_t nspec, const uint32_t *__restrict__ cnt,
+                        uint32_t *__restrict__ cursor, uint32_t *__restrict__ order)
+{
+    __shared__ uint32_t off[kCostClasses];
+    if (threadIdx.x == 0)
+    {
+        uint32_t run = 0;
+        for (int k = kCostClasses - 1; k >= 0; k--)
+        {
+            off[k] = run;
+            run += cnt[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nspec) return;
+    const uint32_t k = cls[s];
+    order[off[k] + atomicAdd(&cursor[k], 1u)] = s;
+}
+
 }  // namespace
 
 size_t search_smem(uint32_t tile, uint32_t dF, bool wide) { return smem_layout(tile, dF, wide).total; }
+
+template <class T>
+static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need);
 
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF)
 {
@@ -793,6 +849,31 @@ uint32_t max_tile(const hc_ctx *ctx, uint32_t dF)
     const size_t room = ctx->smem_optin > extra ? ctx->smem_optin - extra : 0;
     uint32_t t = (uint32_t)(room / 8) & ~511u;
     return t < 512 ? 512 : t;
+}
+
+uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm)
+{
+    if (ctas_per_sm <= 1) return max_tile(ctx, dF);
+    // the SM's shared memory (optin + 1 KB) is split; each CTA keeps 1 KB for the system
+    const size_t per = (ctx->smem_optin + 1024) / ctas_per_sm - 1024;
+    const size_t extra = smem_layout(0, dF, false).total;
+    const size_t room = per > extra ? per - extra : 0;
+    uint32_t t = (uint32_t)(room / 8) & ~511u;
+    return t;
+}
+
+int prepare_query(hc_ctx *ctx, uint32_t nspec)
+{
+    int rc = sync_lengths(ctx);
+    if (rc) return rc;
+    const uint32_t nlen = (uint32_t)ctx->lens.size();
+    QueryScratch &q = ctx->qs;
+    if ((rc = grow(ctx, &q.d_win, &q.win_cap, (size_t)nspec * nlen))) return rc;
+    if ((rc = grow(ctx, &q.d_wide, &q.wide_cap, (size_t)nspec + 4))) return rc;
+    if ((rc = grow(ctx, &q.d_order, &q.order_cap, 2 * (size_t)nspec))) return rc;
+    if ((rc = grow(ctx, &q.d_fitstart, &q.fit_cap, (size_t)nspec))) return rc;
+    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * (4 + 2 * 64)));
+    return HC_SUCCESS;
 }
 
 namespace {
@@ -877,9 +958,12 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     QueryScratch &q = ctx->qs;
     if ((rc = grow(ctx, &q.d_win, &q.win_cap, (size_t)nspec * nlen))) return rc;
     if ((rc = grow(ctx, &q.d_wide, &q.wide_cap, (size_t)nspec + 4))) return rc;
-    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 16));
+    const uint32_t sched = ctx->tuning.schedule;
+    if (sched == 2 && (rc = grow(ctx, &q.d_order, &q.order_cap, 2 * (size_t)nspec))) return rc;
+    if ((rc = grow(ctx, &q.d_fitstart, &q.fit_cap, (size_t)nspec))) return rc;
+    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * (4 + 2 * 64)));
     q.d_nwide = q.d_work + 2;
-    HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 16, st));
+    HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 4 * (4 + 2 * 64), st));
 
     const uint64_t nw = (uint64_t)nspec * nlen;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
@@ -907,8 +991,19 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.nwide = q.d_nwide;
     a.work = q.d_work;
     a.tile = ctx->tuning.tile;
+    a.persistent = sched != 1;
+    int launches = 4;
+    if (sched == 2)
+    {
+        uint32_t *cls = q.d_order + nspec, *cnt = q.d_work + 4, *cur = q.d_work + 4 + 64;
+        k_cost<<<(nspec + 255) / 256, 256, 0, st>>>(q.d_win, nspec, nlen, cls, cnt);
+        k_order<<<(nspec + 255) / 256, 256, 0, st>>>(cls, nspec, cnt, cur, q.d_order);
+        HC_CUDA(ctx, cudaGetLastError());
+        a.order = q.d_order;
+        launches += 2;
+    }
     const size_t smem = search_smem(a.tile, a.dF, false);
-    const int grid = ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
+    const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     int rc2 = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
     if (rc2) return rc2;
@@ -916,19 +1011,20 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     // spectra whose packed scorecard could overflow are redone wide; the
     // list length is read on the device (no host synchronisation)
     SearchArgs b = a;
+    b.persistent = 1;
+    b.order = nullptr;
     b.only = q.d_wide;
     b.nonly_dev = q.d_nwide;
     b.work = q.d_work + 1;
     b.tile = ctx->tuning.tile / 2;
     const size_t smem2 = search_smem(b.tile, b.dF, true);
-    rc2 = launch_search<true>(ctx, b, grid, ctx->tuning.threads, smem2, 2, st);
+    rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
     if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
-                                                                            ctx->p.expect_max);
+                                                                            ctx->p.expect_max, q.d_fitstart);
     HC_CUDA(ctx, cudaGetLastError());
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[4], st));
-    int launches = 4;
     ctx->last_launches = launches;
     return HC_SUCCESS;
 }

@@ -163,3 +163,27 @@ def DSLIM_Construct(index: Index, L_: int, seqs: np.ndarray) -> int:
 def DSLIM_QuerySpectrum(queries, index: Index):
     """dslim.h:184 — search a batch; returns (results, histograms)."""
     return index.query(queries)
+
+
+def _tune_device(ix: Index, d_idx, d_moz, d_int, d_prec, d_dM, nspec, npeaks, d_out, d_hist):
+    """hc_tune on device buffers; returns (tuning dict, best ms)."""
+    t = L.HcTuning()
+    ms = C.c_float()
+    ix._check(ix.lib.hc_tune(ix.ctx, C.c_void_p(d_idx), C.c_void_p(d_moz), C.c_void_p(d_int), C.c_void_p(d_prec),
+                             None if d_dM is None else C.c_void_p(d_dM), nspec, npeaks, C.c_void_p(d_out),
+                             C.c_void_p(d_hist), C.byref(t), C.byref(ms)), "hc_tune")
+    return {k: getattr(t, k) for k, _ in L.HcTuning._fields_}, ms.value
+
+
+Index.tune_device = _tune_device
+
+
+def _query_graph(ix: Index, d_idx, d_moz, d_int, d_prec, d_dM, nspec, npeaks, d_out, d_hist, stream=None):
+    """Batched form: the query pipeline replayed from a captured CUDA graph."""
+    ix._check(ix.lib.hc_dslim_query_graph(
+        ix.ctx, C.c_void_p(d_idx), C.c_void_p(d_moz), C.c_void_p(d_int), C.c_void_p(d_prec),
+        None if d_dM is None else C.c_void_p(d_dM), nspec, npeaks, C.c_void_p(d_out), C.c_void_p(d_hist),
+        None if stream is None else C.c_void_p(stream)), "hc_dslim_query_graph")
+
+
+Index.query_graph = _query_graph

@@ -55,6 +55,7 @@ extern "C" {
 #define HC_FLAG_TAILFIT_OOB 0x4u   /* tail-fit slice starts at -1 (expeRT.cpp:653,690) */
 #define HC_FLAG_TAILFIT_EMPTY 0x8u /* empty tail-fit slice: 0/0 fit (expeRT.cpp:590-601) */
 #define HC_FLAG_WIDE 0x100u        /* scored by the wide-scorecard kernel */
+#define HC_FLAG_LEARNED 0x200u     /* e-value from the learned tail (hc_mlp_evalues) */
 
 /* gParams fields on the DSLIM path (slm_dsts.h:359-418). dF is in bins
  * ((uint)(tolerance_Da * scale), hicops.cpp:564); dM in Da; mod_mass is scaled
@@ -109,6 +110,9 @@ typedef struct hc_tuning
     uint32_t tile;         /* scorecard candidates per shared-memory tile */
     uint32_t ctas_per_sm;  /* resident CTAs per SM the grid is sized for */
     uint32_t pairs_per_warp; /* (peak, bin) postings lists a warp streams at once */
+    uint32_t schedule;     /* 0: persistent CTAs, work stealing in batch order;
+                              1: plain, one CTA per spectrum;
+                              2: batched, persistent CTAs, longest windows first */
 } hc_tuning;
 
 int hc_version(void);
@@ -157,6 +161,19 @@ int hc_dslim_query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_
                           const uint32_t *d_intensity, const float *d_precurse,
                           const double *d_dM, uint32_t nspec, uint32_t npeaks,
                           hc_result *d_out, uint32_t *d_hist, void *stream);
+/* Batched form: the same pipeline captured once into a CUDA graph and
+ * replayed; a call whose buffers, sizes or tuning differ from the captured
+ * one re-captures. Results are identical to hc_dslim_query_device. */
+int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz,
+                         const uint32_t *d_intensity, const float *d_precurse,
+                         const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                         hc_result *d_out, uint32_t *d_hist, void *stream);
+/* Autotuner: times the search on a device-resident sample batch for every
+ * launch shape of a small grid (block size, tile, lists per warp, CTAs per SM,
+ * schedule), keeps the fastest in the context and returns it. */
+int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
+            const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
+            hc_result *d_out, uint32_t *d_hist, hc_tuning *best, float *best_ms);
 /* Host-side check of the postings-id decoding: counts x in [0, xmax) for
  * which the multiply-shift quotient used on the device differs from x / d
  * (0 expected; no device needed). */
