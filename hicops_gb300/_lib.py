@@ -89,6 +89,8 @@ _SIGS = [
                                         C.c_void_p]),
     ("hc_last_launch_count", C.c_int, [C.c_void_p]),
     ("hc_check_division", C.c_uint64, [C.c_uint32, C.c_uint32]),
+    ("hc_ctx_set_phase_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("hc_phase_cycles", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("hc_dslim_query_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),

@@ -143,6 +143,7 @@ int hc_ctx_destroy(hc_ctx *ctx)
     cudaFree(ctx->qs.d_work);
     cudaFree(ctx->qs.d_order);
     cudaFree(ctx->qs.d_fitstart);
+    cudaFree(ctx->d_phase);
     cudaFree(ctx->qs.d_in);
     cudaFree(ctx->qs.d_outbuf);
     for (auto &e : ctx->ev)

@@ -140,4 +140,32 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
     return HC_SUCCESS;
 }
 
+int hc_ctx_set_phase_timing(hc_ctx *ctx, int on)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    cudaSetDevice(ctx->device);
+    if (on && !ctx->d_phase)
+    {
+        HC_CUDA(ctx, cudaMalloc((void **)&ctx->d_phase, 8 * 16));
+        HC_CUDA(ctx, cudaMemset(ctx->d_phase, 0, 8 * 16));
+    }
+    if (!on && ctx->d_phase)
+    {
+        cudaFree(ctx->d_phase);
+        ctx->d_phase = nullptr;
+    }
+    return HC_SUCCESS;
+}
+
+int hc_phase_cycles(hc_ctx *ctx, uint64_t out[10])
+{
+    if (!ctx || !out) return HC_ERR_INVLD_PTR;
+    if (!ctx->d_phase) return set_error(ctx, HC_ERR_INVLD_PARAM, "phase timing is off");
+    HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    HC_CUDA(ctx, cudaDeviceSynchronize());
+    HC_CUDA(ctx, cudaMemcpy(out, ctx->d_phase, 8 * 10, cudaMemcpyDeviceToHost));
+    HC_CUDA(ctx, cudaMemset(ctx->d_phase, 0, 8 * 16));
+    return HC_SUCCESS;
+}
+
 }  // extern "C"

@@ -122,6 +122,7 @@ struct hc_ctx
     bool lens_dirty = true;
     bool profiling = false;
     cudaEvent_t ev[5] = {};  // windows | search | wide | tailfit boundaries
+    unsigned long long *d_phase = nullptr;  // per-phase SM cycles of the search kernel (diagnostics)
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     hc::GraphKey graph_key{};

@@ -59,7 +59,11 @@ struct SearchArgs
     const uint32_t *nonly_dev;  // its length, in device memory
     const uint32_t *order;  // optional processing order (longest first)
     uint32_t persistent;    // 1: CTAs loop over a work counter; 0: one spectrum per CTA
+    unsigned long long *phase;  // optional: SM cycles per phase, summed over CTAs (kPhases)
 };
+
+// phases of k_search timed when SearchArgs::phase is set
+constexpr int kPhases = 6;  // bucket setup | postings stream | score pass 1 | pass 2 | tile clear | rest
 
 __device__ __forceinline__ uint32_t lower_bound_g(const uint32_t *__restrict__ a, uint32_t lo,
                                                   uint32_t hi, uint32_t v)
@@ -130,8 +134,22 @@ struct SmemTail
     uint32_t pnext;            // next postings list to hand out
     uint32_t pad1;
     unsigned long long bytes;
+    unsigned long long ph[kPhases];
+    unsigned long long ph_last;
+    unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations (pass 1)
     float lgf[kLgTable];
 };
+
+// adds the cycles since the last mark to phase k (thread 0 only, after a barrier)
+#define HC_PHASE(k)                                               \
+    do {                                                          \
+        if (a.phase && tid == 0)                                  \
+        {                                                         \
+            const unsigned long long _t = clock64();              \
+            T.ph[(k)] += _t - T.ph_last;                          \
+            T.ph_last = _t;                                       \
+        }                                                         \
+    } while (0)
 
 struct SmemLayout
 {
@@ -152,9 +170,12 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     return o;
 }
 
+// float estimate of the hyperscore; the packed sums are < 2^24, so the
+// integer-to-float conversions stay 32-bit (exact, full-rate)
 __device__ __forceinline__ float approx_h(const float *lgf, uint32_t bc, uint32_t yc, uint64_t ib, uint64_t iy)
 {
-    return ((lgf[bc] + lgf[yc]) + log10f((float)(1 + ib))) + log10f((float)(1 + iy)) - 6.0f;
+    const float fb = __uint2float_rn((uint32_t)ib + 1u), fy = __uint2float_rn((uint32_t)iy + 1u);
+    return ((lgf[bc] + lgf[yc]) + log10f(fb)) + log10f(fy) - 6.0f;
 }
 
 template <bool WIDE>
@@ -186,7 +207,7 @@ __device__ __forceinline__ void decode(const unsigned long long *card, uint32_t 
 // sign or the histogram bin undecided), bin its histogram bin.
 template <bool WIDE>
 __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const float *lgf, uint32_t bc, uint32_t yc,
-                                      uint64_t ib, uint64_t iy, float &h, int &bin)
+                                      uint64_t ib, uint64_t iy, float &h, int &bin, uint32_t &nexact)
 {
     if (!WIDE)
     {
@@ -200,6 +221,7 @@ __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const f
             return ha > 0.0f;
         }
     }
+    nexact++;
     const float hf = exact_h(qc, bc, yc, ib, iy);
     h = hf;
     bin = hist_bin(hf);
@@ -233,6 +255,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
     for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
+    if (tid == 0)
+    {
+        for (int k = 0; k < kPhases; k++) T.ph[k] = 0;
+        for (int k = 0; k < 4; k++) T.cnt[k] = 0;
+        T.ph_last = clock64();
+    }
 
     for (uint32_t iter = 0;; iter++)
     {
@@ -316,6 +344,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
             }
             uint32_t my_inwin = 0;
             __syncthreads();
+            HC_PHASE(0);
 
             for (uint32_t c0 = (uint32_t)w.x; c0 <= (uint32_t)w.y; c0 += tile)
             {
@@ -421,12 +450,20 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                     }
                 }
                 __syncthreads();
+                HC_PHASE(1);
                 // ---- score the candidates that reached min_shp ----
                 // pass 1: hyperscore (float, exact where the bound leaves the
                 // sign or the bin open), cpsms, histogram, tile maximum
                 const uint32_t qn = T.qcount;
                 const bool scan_all = WIDE || qn > (uint32_t)kQcap || a.thr > 250;
                 const uint32_t nscore = scan_all ? (c1 - c0) : qn;
+                uint32_t my_exact = 0;
+                if (a.phase && tid == 0)
+                {
+                    T.cnt[0] += 1;
+                    T.cnt[1] += scan_all ? 1 : 0;
+                    T.cnt[2] += qn;
+                }
                 float my_max = 0.0f;
                 uint32_t my_cps = 0, my_fl = 0;
                 for (uint32_t i = tid; i < nscore; i += nthr)
@@ -438,7 +475,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                     if (shp < a.min_shp || shp == 0) continue;
                     float h;
                     int bin;
-                    if (!score<WIDE>(a.qc, T.lgf, bc, yc, ib, iy, h, bin)) continue;
+                    if (!score<WIDE>(a.qc, T.lgf, bc, yc, ib, iy, h, bin, my_exact)) continue;
                     my_cps++;
                     if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
                     if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
@@ -446,9 +483,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                     my_max = fmaxf(my_max, h);
                 }
                 if (my_cps) atomicAdd(&T.cpsms, my_cps);
+                if (a.phase && my_exact) atomicAdd(&T.cnt[3], (unsigned long long)my_exact);
                 if (my_fl) atomicOr(&T.flags, my_fl);
                 if (my_max > 0.0f) atomicMax(&T.maxbits, __float_as_uint(my_max));
                 __syncthreads();
+                HC_PHASE(2);
                 // pass 2: the reference's double hyperscore for every candidate
                 // that can still be the top hit (within kNear of the maximum so far)
                 {
@@ -478,6 +517,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                         }
                 }
                 __syncthreads();
+                HC_PHASE(3);
                 if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
                 // ---- clear the tile ----
                 {
@@ -492,10 +532,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                     T.pnext = 0;
                 }
                 __syncthreads();
+                HC_PHASE(4);
             }
             if (my_inwin) atomicAdd(&T.bytes, 4ull * my_inwin);
         }
         __syncthreads();  // every thread's byte count is in before thread 0 reads it
+        HC_PHASE(5);
         // ---- write the spectrum's results ----
         if (!WIDE && T.overflow)
         {
@@ -535,6 +577,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
             r.evalue = 0.0;
             a.out[s] = r;
         }
+    }
+    if (a.phase && tid == 0)
+    {
+        for (int k = 0; k < kPhases; k++) atomicAdd(&a.phase[k], T.ph[k]);
+        for (int k = 0; k < 4; k++) atomicAdd(&a.phase[kPhases + k], T.cnt[k]);
     }
 }
 
@@ -992,6 +1039,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.work = q.d_work;
     a.tile = ctx->tuning.tile;
     a.persistent = sched != 1;
+    a.phase = ctx->d_phase;
     int launches = 4;
     if (sched == 2)
     {
@@ -1012,6 +1060,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     // list length is read on the device (no host synchronisation)
     SearchArgs b = a;
     b.persistent = 1;
+    b.phase = nullptr;
     b.order = nullptr;
     b.only = q.d_wide;
     b.nonly_dev = q.d_nwide;

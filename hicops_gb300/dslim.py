@@ -187,3 +187,19 @@ def _query_graph(ix: Index, d_idx, d_moz, d_int, d_prec, d_dM, nspec, npeaks, d_
 
 
 Index.query_graph = _query_graph
+
+
+def _phase_cycles(ix: Index) -> dict:
+    """Summed SM cycles per search-kernel phase since the last call (phase timing on)."""
+    out = (C.c_uint64 * 10)()
+    ix._check(ix.lib.hc_phase_cycles(ix.ctx, out), "hc_phase_cycles")
+    return dict(zip(("setup", "stream", "score1", "score2", "clear", "rest", "n_tiles", "n_tiles_scanned",
+                     "n_listed", "n_exact"), list(out)))
+
+
+def _set_phase_timing(ix: Index, on: bool = True):
+    ix._check(ix.lib.hc_ctx_set_phase_timing(ix.ctx, int(on)), "hc_ctx_set_phase_timing")
+
+
+Index.phase_cycles = _phase_cycles
+Index.set_phase_timing = _set_phase_timing

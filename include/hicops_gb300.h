@@ -174,6 +174,13 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
 int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
             const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
             hc_result *d_out, uint32_t *d_hist, hc_tuning *best, float *best_ms);
+/* Diagnostics: with phase timing on, the search kernel adds up SM clock
+ * cycles per phase (bucket setup, postings stream, score pass 1, score pass 2,
+ * tile clear, rest) over all CTAs, then four counts (tiles, tiles scored by a
+ * whole-tile scan, listed candidates, exact hyperscores in pass 1);
+ * hc_phase_cycles returns and clears them. */
+int hc_ctx_set_phase_timing(hc_ctx *ctx, int on);
+int hc_phase_cycles(hc_ctx *ctx, uint64_t out[10]);
 /* Host-side check of the postings-id decoding: counts x in [0, xmax) for
  * which the multiply-shift quotient used on the device differs from x / d
  * (0 expected; no device needed). */
