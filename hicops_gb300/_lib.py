@@ -90,6 +90,20 @@ _SIGS = [
     ("hc_last_launch_count", C.c_int, [C.c_void_p]),
     ("hc_check_division", C.c_uint64, [C.c_uint32, C.c_uint32]),
     ("hc_ctx_set_phase_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("hc_mlp_create", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("hc_mlp_destroy", C.c_int, [C.c_void_p]),
+    ("hc_mlp_num_params", C.c_int, []),
+    ("hc_mlp_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("hc_mlp_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("hc_mlp_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_targets", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_gradients", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                   C.POINTER(C.c_float)]),
+    ("hc_mlp_train", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
+                               C.POINTER(C.c_float)]),
+    ("hc_mlp_evalues", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]),
     ("hc_phase_cycles", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("hc_dslim_query_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,

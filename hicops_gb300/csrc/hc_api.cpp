@@ -108,6 +108,17 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     make_ion_tables(ctx->p, &ctx->tables);
     QueryConst qc;
     make_query_const(&qc);
+    {
+        std::vector<double> lt(kLog10Tab);
+        make_log10_table(lt.data(), kLog10Tab);
+        if (cudaMalloc((void **)&ctx->d_log10, sizeof(double) * kLog10Tab) != cudaSuccess ||
+            cudaMemcpy(ctx->d_log10, lt.data(), sizeof(double) * kLog10Tab, cudaMemcpyHostToDevice) != cudaSuccess)
+        {
+            hc_ctx_destroy(ctx);
+            return HC_ERR_BAD_MEM_ALLOC;
+        }
+        qc.log10_tab = ctx->d_log10;
+    }
     if (cudaMalloc((void **)&ctx->d_tables, sizeof(IonTables)) != cudaSuccess ||
         cudaMalloc((void **)&ctx->d_qconst, sizeof(QueryConst)) != cudaSuccess ||
         cudaMemcpy(ctx->d_tables, &ctx->tables, sizeof(IonTables), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -144,6 +155,7 @@ int hc_ctx_destroy(hc_ctx *ctx)
     cudaFree(ctx->qs.d_order);
     cudaFree(ctx->qs.d_fitstart);
     cudaFree(ctx->d_phase);
+    cudaFree(ctx->d_log10);
     cudaFree(ctx->qs.d_in);
     cudaFree(ctx->qs.d_outbuf);
     for (auto &e : ctx->ev)

@@ -5,8 +5,10 @@
 // Compiled with -ffp-contract=off: the tables are derived with the same
 // double arithmetic the reference uses, and must round the same way on
 // x86-64 and aarch64.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "hc_internal.h"
 
@@ -141,6 +143,21 @@ void make_query_const(QueryConst *q)
         q->lgfact[i] = std::log10((double)i) + q->lgfact[i - 1];
     for (int i = 0; i < kLgTable; i++)
         q->lgfact_f[i] = (float)q->lgfact[i];
+    q->log10_tab = nullptr;
+}
+
+void make_log10_table(double *t, uint32_t n)
+{
+    // log10(n) for the integers the hyperscore takes logarithms of
+    // (log10(1 + ibc), dslim_query.cpp:698), from the host's libm: the same
+    // function the reference calls. Filled by all host threads.
+    const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned k = 0; k < nt; k++)
+        th.emplace_back([=]() {
+            for (uint32_t i = k; i < n; i += nt) t[i] = std::log10((double)i);
+        });
+    for (auto &x : th) x.join();
 }
 
 int64_t make_entries(const hc_params &p, uint32_t L, const uint8_t *seqs, uint32_t npep,

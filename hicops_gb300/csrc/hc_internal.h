@@ -47,10 +47,13 @@ struct IonTables
     uint32_t maxz, scale, min_mass, max_mass;
 };
 
+constexpr uint32_t kLog10Tab = 1u << 24;  // log10(n) for every n the packed sums can reach
+
 struct QueryConst
 {
     double lgfact[kLgTable];   // log10(n!) exactly as utils.h:115-131 builds it
     float lgfact_f[kLgTable];  // the same, rounded to float (fast path)
+    const double *log10_tab;   // device table: log10_tab[n] = log10(n), n < kLog10Tab (host libm values)
 };
 
 // Host-side record of one length.
@@ -123,6 +126,7 @@ struct hc_ctx
     bool profiling = false;
     cudaEvent_t ev[5] = {};  // windows | search | wide | tailfit boundaries
     unsigned long long *d_phase = nullptr;  // per-phase SM cycles of the search kernel (diagnostics)
+    double *d_log10 = nullptr;              // log10 table of the exact hyperscore path
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     hc::GraphKey graph_key{};
@@ -134,6 +138,7 @@ namespace hc {
 // hc_host.cpp
 void make_ion_tables(const hc_params &p, IonTables *t);
 void make_query_const(QueryConst *q);
+void make_log10_table(double *t, uint32_t n);
 int64_t make_entries(const hc_params &p, uint32_t L, const uint8_t *seqs, uint32_t npep,
                      hc_entry *out, int64_t cap);
 void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);

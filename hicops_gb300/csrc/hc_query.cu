@@ -84,10 +84,14 @@ __device__ __forceinline__ float exact_h(const QueryConst *__restrict__ qc, uint
 {
     const double h1 = __dadd_rn(qc->lgfact[bc < kLgTable ? bc : kLgTable - 1],
                                 qc->lgfact[yc < kLgTable ? yc : kLgTable - 1]);
-    double h = __dadd_rn(h1, log10((double)(1 + ib)));
-    h = __dadd_rn(h, log10((double)(1 + iy)));
+    // log10 of the intensity sums from the host-built table (the device's
+    // double log10 is very slow on this part); beyond it, the device log10
+    const double lb = (1 + ib < kLog10Tab) ? __ldg(qc->log10_tab + 1 + ib) : log10((double)(1 + ib));
+    const double ly = (1 + iy < kLog10Tab) ? __ldg(qc->log10_tab + 1 + iy) : log10((double)(1 + iy));
+    double h = __dadd_rn(h1, lb);
+    h = __dadd_rn(h, ly);
     h = __dadd_rn(h, -6.0);
-    return (float)h;
+    return __double2float_rn(h);
 }
 
 // histogram bin (int)(h*10 + 0.5): a float product, then a double sum

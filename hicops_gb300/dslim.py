@@ -203,3 +203,62 @@ def _set_phase_timing(ix: Index, on: bool = True):
 
 Index.phase_cycles = _phase_cycles
 Index.set_phase_timing = _set_phase_timing
+
+
+class MLP:
+    """The learned e-value tail (256 -> 128 -> 64 -> 3), on the device of an Index."""
+
+    N_IN, N_OUT = 256, 3
+
+    def __init__(self, ix: Index, seed: int = 1):
+        self.ix = ix
+        h = C.c_void_p()
+        ix._check(ix.lib.hc_mlp_create(ix.ctx, C.c_uint64(seed), C.byref(h)), "hc_mlp_create")
+        self.h = h
+        self.nparams = ix.lib.hc_mlp_num_params()
+
+    def close(self):
+        if self.h:
+            self.ix.lib.hc_mlp_destroy(self.h)
+            self.h = None
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, np.float32)
+        self.ix._check(self.ix.lib.hc_mlp_get_params(self.h, L.ptr(out)), "hc_mlp_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        self.ix._check(self.ix.lib.hc_mlp_set_params(self.h, L.ptr(p)), "hc_mlp_set_params")
+
+    def gradients(self, d_X: int, d_Y: int, n: int):
+        g = np.zeros(self.nparams, np.float32)
+        loss = C.c_float()
+        self.ix._check(self.ix.lib.hc_mlp_gradients(self.h, C.c_void_p(d_X), C.c_void_p(d_Y), n, L.ptr(g),
+                                                    C.byref(loss)), "hc_mlp_gradients")
+        return g, loss.value
+
+    def train(self, d_X: int, d_Y: int, n: int, batch: int = 4096, epochs: int = 1, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        self.ix._check(self.ix.lib.hc_mlp_train(self.h, C.c_void_p(d_X), C.c_void_p(d_Y), n, batch, epochs,
+                                                C.c_float(lr), C.byref(loss)), "hc_mlp_train")
+        return loss.value
+
+    def forward(self, d_X: int, n: int, d_out: int, stream: int | None = None):
+        self.ix._check(self.ix.lib.hc_mlp_forward(self.h, C.c_void_p(d_X), n, C.c_void_p(d_out),
+                                                  None if stream is None else C.c_void_p(stream)), "hc_mlp_forward")
+
+    def features(self, d_hist: int, d_res: int, n: int, d_X: int, stream: int | None = None):
+        self.ix._check(self.ix.lib.hc_mlp_features(self.ix.ctx, C.c_void_p(d_hist), C.c_void_p(d_res), n,
+                                                   C.c_void_p(d_X), None if stream is None else C.c_void_p(stream)),
+                       "hc_mlp_features")
+
+    def targets(self, d_res: int, n: int, d_Y: int, stream: int | None = None):
+        self.ix._check(self.ix.lib.hc_mlp_targets(self.ix.ctx, C.c_void_p(d_res), n, C.c_void_p(d_Y),
+                                                  None if stream is None else C.c_void_p(stream)), "hc_mlp_targets")
+
+    def evalues(self, d_X: int, d_res: int, n: int, thresh: float, d_learned: int, d_nfb: int, d_scratch: int,
+                stream: int | None = None):
+        self.ix._check(self.ix.lib.hc_mlp_evalues(self.h, C.c_void_p(d_X), C.c_void_p(d_res), n, C.c_float(thresh),
+                                                  C.c_void_p(d_learned), C.c_void_p(d_nfb), C.c_void_p(d_scratch),
+                                                  None if stream is None else C.c_void_p(stream)), "hc_mlp_evalues")

@@ -174,6 +174,37 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
 int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
             const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
             hc_result *d_out, uint32_t *d_hist, hc_tuning *best, float *best_ms);
+/* ---- learned e-value tail (no reference counterpart; replaces the
+ * per-spectrum regression of expeRT::ModelTailFit, expeRT.cpp:572-718, which
+ * stays the fallback and the judge) ----
+ * A 256 -> 128 -> 64 -> 3 FP32 MLP mapping a spectrum's histogram (as its log
+ * survival curve, bins >= 255 folded) to the tail line (slope, intercept,
+ * first regression bin). Parameters: W1[256x128] b1 W2[128x64] b2 W3[64x3] b3. */
+typedef struct hc_mlp hc_mlp;
+int hc_mlp_create(hc_ctx *ctx, uint64_t seed, hc_mlp **out);
+int hc_mlp_destroy(hc_mlp *m);
+int hc_mlp_num_params(void);
+int hc_mlp_get_params(hc_mlp *m, float *host);
+int hc_mlp_set_params(hc_mlp *m, const float *host);
+/* X[n,256] from the histograms and results of a query (device buffers). */
+int hc_mlp_features(hc_ctx *ctx, const uint32_t *d_hist, const hc_result *d_res, uint32_t n, float *d_X,
+                    void *stream);
+/* Y[n,3] = the expeRT fit (slope, intercept, first bin) of the context's last query. */
+int hc_mlp_targets(hc_ctx *ctx, const hc_result *d_res, uint32_t n, float *d_Y, void *stream);
+int hc_mlp_forward(hc_mlp *m, const float *d_X, uint32_t n, float *d_out, void *stream);
+/* Gradients of the mean squared error (scaled targets) over one batch, to host. */
+int hc_mlp_gradients(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, float *host_grads,
+                     float *loss);
+/* Adam training over [0, n) in minibatches of `batch` for `epochs`. */
+int hc_mlp_train(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, uint32_t batch,
+                 uint32_t epochs, float lr, float *final_loss);
+/* Learned e-values: where the predicted line fits the spectrum's survival
+ * curve within `thresh` (RMS, log10 units) its e-value replaces the expeRT one
+ * in d_res (flag HC_FLAG_LEARNED); elsewhere the expeRT value stays and
+ * *d_nfallback counts it. d_learned_log10e[n] gets the prediction for every
+ * spectrum; d_out_scratch holds n*3 floats. */
+int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh,
+                   float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
 /* Diagnostics: with phase timing on, the search kernel adds up SM clock
  * cycles per phase (bucket setup, postings stream, score pass 1, score pass 2,
  * tile clear, rest) over all CTAs, then four counts (tiles, tiles scored by a
