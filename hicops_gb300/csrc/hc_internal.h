@@ -89,6 +89,17 @@ struct QueryScratch
     size_t out_cap = 0;
 };
 
+// Caller-supplied scratch of one query (see launch_query_scratch).
+struct ScratchPtrs
+{
+    int2 *win;          // nspec * nlen
+    uint32_t *wide;     // nspec + 4
+    uint32_t *work;     // 4 + 2 * 64
+    uint32_t *order;    // 2 * nspec
+    int32_t *fitstart;  // nspec
+    LenDev *lens;       // HC_MAX_LENGTHS
+};
+
 // What a captured query graph was recorded with; a call that differs re-captures.
 struct GraphKey
 {
@@ -155,6 +166,9 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
                  hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);
 int sync_lengths(hc_ctx *ctx);
+int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
+                         const float *d_prec, const double *d_dM, uint32_t nspec, hc_result *d_out,
+                         uint32_t *d_hist, const ScratchPtrs &s, cudaStream_t st);
 
 int set_error(hc_ctx *ctx, int code, const std::string &msg);
 int cuda_check(hc_ctx *ctx, cudaError_t e, const char *what);

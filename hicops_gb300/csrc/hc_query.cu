@@ -1082,4 +1082,93 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     return HC_SUCCESS;
 }
 
+// The query pipeline of query_device with every scratch buffer supplied by
+// the caller (used by the allocation-free entry point): the length table is
+// copied into s.lens, nothing is allocated and the host does not wait.
+int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
+                         const float *d_prec, const double *d_dM, uint32_t nspec, hc_result *d_out,
+                         uint32_t *d_hist, const ScratchPtrs &s, cudaStream_t st)
+{
+    const uint32_t nlen = (uint32_t)ctx->lens.size();
+    LenDev h[HC_MAX_LENGTHS];
+    for (uint32_t i = 0; i < nlen; i++)
+    {
+        const LenHost &lh = ctx->lens[i];
+        LenDev &d = h[i];
+        std::memset(&d, 0, sizeof(d));
+        d.L = lh.L;
+        d.n = lh.built ? lh.n : 0;
+        d.npep = lh.npep;
+        d.speclen = 2 * ctx->p.maxz * (lh.L - 1);
+        d.half = d.speclen / 2;
+        division_magic(d.speclen, &d.magic, &d.msh);
+        d.mass = lh.d_mass;
+        d.seqid = lh.d_seqid;
+        d.sites = lh.d_sites;
+        d.modnum = lh.d_modnum;
+        d.seqs = lh.d_seqs;
+        d.bA = lh.d_bA;
+        d.iA = lh.d_iA;
+    }
+    // pageable source: the copy is staged before the call returns
+    HC_CUDA(ctx, cudaMemcpyAsync(s.lens, h, sizeof(LenDev) * nlen, cudaMemcpyHostToDevice, st));
+    ctx->last_launches = 0;
+    if (nspec == 0) return HC_SUCCESS;
+    uint32_t *nwide = s.work + 2;
+    HC_CUDA(ctx, cudaMemsetAsync(s.work, 0, 4 * (4 + 2 * 64), st));
+    const uint64_t nw = (uint64_t)nspec * nlen;
+    k_windows<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(s.lens, nlen, d_prec, d_dM, ctx->p.dM, nspec, s.win);
+    HC_CUDA(ctx, cudaGetLastError());
+    SearchArgs a{};
+    a.lens = s.lens;
+    a.nlen = nlen;
+    a.qc = ctx->d_qconst;
+    a.idx = d_idx;
+    a.moz = d_moz;
+    a.inten = d_int;
+    a.prec = d_prec;
+    a.win = s.win;
+    a.nspec = nspec;
+    a.dF = ctx->p.dF;
+    a.min_shp = ctx->p.min_shp;
+    a.thr = ctx->p.min_shp > 0 ? ctx->p.min_shp : 1;
+    a.maxbin = ctx->p.max_mass * ctx->p.scale;
+    a.out = d_out;
+    a.hist = d_hist;
+    a.wide_list = s.wide;
+    a.nwide = nwide;
+    a.work = s.work;
+    a.tile = ctx->tuning.tile;
+    const uint32_t sched = ctx->tuning.schedule;
+    a.persistent = sched != 1;
+    int launches = 4;
+    if (sched == 2)
+    {
+        uint32_t *cls = s.order + nspec, *cnt = s.work + 4, *cur = s.work + 4 + 64;
+        k_cost<<<(nspec + 255) / 256, 256, 0, st>>>(s.win, nspec, nlen, cls, cnt);
+        k_order<<<(nspec + 255) / 256, 256, 0, st>>>(cls, nspec, cnt, cur, s.order);
+        HC_CUDA(ctx, cudaGetLastError());
+        a.order = s.order;
+        launches += 2;
+    }
+    const size_t smem = search_smem(a.tile, a.dF, false);
+    const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
+    int rc = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
+    if (rc) return rc;
+    SearchArgs b = a;
+    b.persistent = 1;
+    b.order = nullptr;
+    b.only = s.wide;
+    b.nonly_dev = nwide;
+    b.work = s.work + 1;
+    b.tile = ctx->tuning.tile / 2;
+    rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true), 2, st);
+    if (rc) return rc;
+    k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
+                                                                            ctx->p.expect_max, s.fitstart);
+    HC_CUDA(ctx, cudaGetLastError());
+    ctx->last_launches = launches;
+    return HC_SUCCESS;
+}
+
 }  // namespace hc

@@ -168,6 +168,17 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
                          const uint32_t *d_intensity, const float *d_precurse,
                          const double *d_dM, uint32_t nspec, uint32_t npeaks,
                          hc_result *d_out, uint32_t *d_hist, void *stream);
+/* Allocation-free form of hc_dslim_query_device (no reference counterpart):
+ * same arguments and results, but its scratch is a fixed file-scope device
+ * array, so it never allocates, for callers that may not allocate device
+ * memory while they search. At most 16384 spectra per call (larger batches
+ * return HC_ERR_INVLD_SIZE). The first call on a device sets up the scratch
+ * address and should come before any stream capture. All calls on one device
+ * share the scratch: calls that overlap on the GPU race. */
+int hc_dslim_query_noalloc(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz,
+                           const uint32_t *d_intensity, const float *d_precurse,
+                           const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                           hc_result *d_out, uint32_t *d_hist, void *stream);
 /* Autotuner: times the search on a device-resident sample batch for every
  * launch shape of a small grid (block size, tile, lists per warp, CTAs per SM,
  * schedule), keeps the fastest in the context and returns it. */
