@@ -30,6 +30,7 @@ static void free_len(LenHost &lh)
     cudaFree(lh.d_seqs);
     cudaFree(lh.d_bA);
     cudaFree(lh.d_iA);
+    cudaFree(lh.d_rows);
     const uint32_t L = lh.L;
     lh = LenHost();
     lh.L = L;
@@ -172,7 +173,7 @@ const char *hc_last_error(const hc_ctx *ctx) { return ctx ? ctx->last_error.c_st
 int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
 {
     if (!ctx || !t) return HC_ERR_INVLD_PTR;
-    if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < 256 || (t->tile & 1) ||
+    if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < kRowG || (t->tile % kRowG) ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
         (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8) ||
         t->schedule > 2)
@@ -287,6 +288,7 @@ int hc_dslim_load(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep, c
     HC_CUDA(ctx, cudaMemcpy(lh->d_bA, bA, 4ull * (nb + 1), cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_iA, iA, 4 * M, cudaMemcpyHostToDevice));
     lh->npost = M;
+    if (const int rt = build_row_table(ctx, *lh)) return rt;
     lh->built = true;
     ctx->lens_dirty = true;
     return HC_SUCCESS;

@@ -93,7 +93,7 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
                     t.schedule = sched;
                     // two resident CTAs share the SM's shared memory
                     t.tile = cps == 1 ? full : (max_tile_for(ctx, ctx->p.dF, cps));
-                    if (t.tile < 1024) continue;
+                    if (t.tile < kRowG) continue;
                     cand.push_back(t);
                 }
     cudaEvent_t e0, e1;

@@ -12,6 +12,8 @@
 //      dslim.cpp:97-125).
 #include <cstdio>
 
+#include <algorithm>
+
 #include "hc_internal.h"
 
 namespace hc {
@@ -344,6 +346,33 @@ __global__ void k_bucket_bounds(const uint32_t *__restrict__ skeys, size_t M, ui
     for (int64_t b = prev + 1; b <= cur; b++) bA[b] = (uint32_t)i;
 }
 
+// Row table: rows[b * stride + k] = first position in bucket b whose entry
+// is >= k * kRowG (ids ascend inside a bucket, so a lower bound on
+// k * kRowG * speclen). Column 0 is bA[b], column stride-1 is bA[b+1].
+__global__ void k_row_table(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ iA, uint32_t nb,
+                            uint32_t stride, uint32_t n, uint32_t speclen, uint32_t *__restrict__ rows)
+{
+    const uint64_t total = (uint64_t)nb * stride;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t b = (uint32_t)(t / stride), k = (uint32_t)(t - (uint64_t)b * stride);
+        uint32_t lo = __ldg(bA + b), hi = __ldg(bA + b + 1);
+        if (k == stride - 1) lo = hi;
+        else if (k > 0)
+        {
+            const uint32_t v = min(k * kRowG, n) * speclen;  // < 2^31
+            while (lo < hi)
+            {
+                const uint32_t m = lo + ((hi - lo) >> 1);
+                if (__ldg(iA + m) < v) lo = m + 1;
+                else hi = m;
+            }
+        }
+        rows[t] = lo;
+    }
+}
+
 template <class T>
 cudaError_t dalloc(T **p, size_t n)
 {
@@ -464,9 +493,27 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         cudaFree(d_site0);
     }
     lh.npost = M;
+    int rc = build_row_table(ctx, lh);
+    if (rc) return rc;
     lh.built = true;
     ctx->lens_dirty = true;
-    ctx->last_launches = launches;
+    ctx->last_launches = launches + 1;
+    return HC_SUCCESS;
+}
+
+int build_row_table(hc_ctx *ctx, LenHost &lh)
+{
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
+    cudaFree(lh.d_rows);
+    lh.d_rows = nullptr;
+    lh.stride = (lh.n + kRowG - 1) / kRowG + 1;
+    HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
+    const uint64_t total = (uint64_t)nb * lh.stride;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)ctx->sm_count * 64);
+    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_bA, lh.d_iA, nb, lh.stride, lh.n, speclen, lh.d_rows);
+    HC_CUDA(ctx, cudaGetLastError());
+    HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HC_SUCCESS;
 }
 

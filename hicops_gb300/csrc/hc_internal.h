@@ -16,6 +16,10 @@ constexpr int kMaxZ = 8;           // fragment charges handled (the reference cl
 constexpr int kLgTable = 256;      // lgfact entries kept on the device (flagged past 80)
 constexpr int kRefMaxShp = 81;     // MAX_SHDPEAKS + 1 (utils.h:110)
 constexpr size_t kIaPad = 128;     // postings arrays are padded: the query reads aligned 16-byte groups
+// Row table: for every bucket, the position of its first posting whose entry
+// is >= k * kRowG, for k = 0 .. ceil(n / kRowG). Scorecard tiles are whole
+// multiples of kRowG entries, so every interior tile boundary is a lookup.
+constexpr uint32_t kRowG = 2048;
 
 // One peptide length's device-resident index. All arrays are device pointers.
 struct LenDev
@@ -23,7 +27,7 @@ struct LenDev
     uint32_t L, speclen, half, n;  // n = entries
     uint32_t npep;
     uint32_t magic, msh;           // floor(x / speclen) = umulhi(x, magic) >> msh, x < 2^31
-    uint32_t pad;
+    uint32_t stride;               // row-table entries per bucket: ceil(n / kRowG) + 1
     const float *mass;
     const uint32_t *seqid;
     const uint64_t *sites;
@@ -31,6 +35,7 @@ struct LenDev
     const uint8_t *seqs;
     const uint32_t *bA;
     const uint32_t *iA;
+    const uint32_t *rows;          // row table, [bucket][k] with `stride` entries per bucket
 };
 
 // Integer ion-key tables, derived on the host with the reference's double
@@ -68,6 +73,8 @@ struct LenHost
     uint8_t *d_seqs = nullptr;
     uint32_t *d_bA = nullptr;
     uint32_t *d_iA = nullptr;
+    uint32_t *d_rows = nullptr;  // row table (max_mass*scale buckets x stride)
+    uint32_t stride = 0;
     bool built = false;
 };
 
@@ -156,6 +163,7 @@ void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
 
 // hc_index.cu
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
+int build_row_table(hc_ctx *ctx, LenHost &lh);
 
 // hc_query.cu
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF);

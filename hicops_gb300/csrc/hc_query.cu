@@ -26,6 +26,7 @@
 // decision open (sign, histogram bin, or a candidate that can still be the
 // top hit) the reference's double expression is evaluated, so cpsms, the
 // histogram and the top hit equal the reference's double evaluation.
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 #include <cstdio>
@@ -36,6 +37,7 @@ namespace hc {
 namespace {
 
 constexpr int kQcap = 3072;         // qualifying-candidate list per tile
+constexpr uint32_t kChunk = 512;    // postings a warp takes at a time
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
 constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
@@ -135,12 +137,13 @@ struct SmemTail
     uint32_t overflow;
     uint32_t spec;
     uint32_t nv;
-    uint32_t pnext;            // next postings list to hand out
+    uint32_t pnext;            // next posting (of the tile's lists laid end to end) to hand out
     uint32_t pad1;
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
     unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations (pass 1)
+    uint32_t wsum[32];         // block scan
     float lgf[kLgTable];
 };
 
@@ -157,7 +160,7 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, pcur, pend, pmoz, pint, tail, total;
+    size_t qual, lstart, lend, loff, pmoz, pint, tail, total;
 };
 
 __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide)
@@ -165,9 +168,10 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
     o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
-    o.pcur = o.qual + 4ull * kQcap;
-    o.pend = o.pcur + 4 * maxpairs;
-    o.pmoz = o.pend + 4 * maxpairs;
+    o.lstart = o.qual + 4ull * kQcap;
+    o.lend = o.lstart + 4 * maxpairs;
+    o.loff = o.lend + 4 * maxpairs;
+    o.pmoz = o.loff + 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.tail = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
     o.total = o.tail + sizeof(SmemTail);
@@ -232,9 +236,74 @@ __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const f
     return hf > 0.0f;
 }
 
-__device__ __forceinline__ uint4 ldg4(const uint32_t *p)
+// Position in a bucket of its first posting whose entry is >= c: a row-table
+// entry when c is a multiple of kRowG, else a search inside that row.
+__device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, const uint32_t *__restrict__ iA,
+                                           uint32_t c, uint32_t speclen)
 {
-    return __ldg(reinterpret_cast<const uint4 *>(p));
+    const uint32_t k = c / kRowG;
+    const uint32_t lo = __ldg(col + k);
+    if (c == k * kRowG) return lo;
+    return lower_bound_g(iA, lo, __ldg(col + k + 1), c * speclen);
+}
+
+// In-place exclusive prefix sum of v[0, n) over the block; v[n] = total,
+// which is also returned. Every thread of the block must call it.
+__device__ uint32_t block_exclusive_scan(uint32_t *v, uint32_t n, uint32_t *wsum)
+{
+    const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
+    const uint32_t per = (n + nthr - 1) / nthr;
+    const uint32_t b = min(n, tid * per), e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += v[i];
+    uint32_t x = sum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0)
+    {
+        uint32_t y = lane < nw ? wsum[lane] : 0u;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t z = __shfl_up_sync(0xFFFFFFFFu, y, o);
+            if (lane >= o) y += z;
+        }
+        if (lane < nw) wsum[lane] = y;
+    }
+    __syncthreads();
+    uint32_t run = x - sum + (wid ? wsum[wid - 1] : 0u);
+    for (uint32_t i = b; i < e; i++)
+    {
+        const uint32_t t = v[i];
+        v[i] = run;
+        run += t;
+    }
+    const uint32_t total = wsum[nw - 1];
+    if (tid == 0) v[n] = total;
+    __syncthreads();
+    return total;
+}
+
+// The last list i in [0, n) with off[i] <= q (off ascending, off[0] = 0):
+// a 32-way search, one shared-memory read per lane per round.
+__device__ __forceinline__ uint32_t find_list(const uint32_t *off, uint32_t n, uint32_t q, int lane)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1)
+    {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t i = lo + (uint32_t)lane * step;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, i < hi && off[i] <= q);
+        lo += (uint32_t)(31 - __clz(m)) * step;
+        hi = min(hi, lo + step);
+    }
+    return lo;
 }
 
 template <bool WIDE, int G>
@@ -248,8 +317,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
     const SmemLayout L = smem_layout(tile, a.dF, WIDE);
     W *card = reinterpret_cast<W *>(smem);
     uint32_t *qual = reinterpret_cast<uint32_t *>(smem + L.qual);
-    uint32_t *pcur = reinterpret_cast<uint32_t *>(smem + L.pcur);
-    uint32_t *pend = reinterpret_cast<uint32_t *>(smem + L.pend);
+    uint32_t *lstart = reinterpret_cast<uint32_t *>(smem + L.lstart);
+    uint32_t *lend = reinterpret_cast<uint32_t *>(smem + L.lend);
+    uint32_t *loff = reinterpret_cast<uint32_t *>(smem + L.loff);
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
@@ -264,6 +334,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
         for (int k = 0; k < kPhases; k++) T.ph[k] = 0;
         for (int k = 0; k < 4; k++) T.cnt[k] = 0;
         T.ph_last = clock64();
+        T.pnext = 0;   // reset again after every tile
+        T.qcount = 0;
     }
 
     for (uint32_t iter = 0;; iter++)
@@ -324,133 +396,109 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
             const int2 w = a.win[(size_t)s * a.nlen + l];
             if (w.x > w.y) continue;
             const LenDev d = a.lens[l];
-            const uint32_t lo_id = (uint32_t)w.x * d.speclen;
-            // A window covering a quarter of the length or more is entered at
-            // each bucket's start: postings below the window are read and
-            // dropped by the tile bound below (cheaper than a dependent
-            // binary search per bucket). Narrower windows search their start.
-            const bool skip_in_stream = 4ull * (uint64_t)(w.y - w.x + 1) >= (uint64_t)d.n;
-            for (uint32_t pr = tid; pr < np; pr += nthr)
+            // bA reads of the reference: two per (peak, bin), one more per peak
+            if (tid == 0) T.bytes += 4ull * (2 * a.dF + 2) * nv;
+            // tiles are aligned to multiples of the tile size, so their
+            // interior boundaries are row-table entries; only the window's
+            // own ends are searched (inside one row)
+            const uint32_t t_first = (uint32_t)w.x / tile, t_last = (uint32_t)w.y / tile;
+            for (uint32_t t = t_first; t <= t_last; t++)
             {
-                const uint32_t k = pr / nbin, j = pr - k * nbin;
-                const uint32_t bin = pmoz[k] - a.dF + j;
-                const uint32_t st = __ldg(d.bA + bin), en = __ldg(d.bA + bin + 1);
-                uint32_t c = st;
-                if (!skip_in_stream && en > st && __ldg(d.iA + st) < lo_id)
-                    c = lower_bound_g(d.iA, st + 1, en, lo_id);
-                pcur[pr] = c;
-                pend[pr] = en;
-            }
-            if (tid == 0)
-            {
-                atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);
-                T.pnext = 0;
-            }
-            uint32_t my_inwin = 0;
-            __syncthreads();
-            HC_PHASE(0);
-
-            for (uint32_t c0 = (uint32_t)w.x; c0 <= (uint32_t)w.y; c0 += tile)
-            {
-                const uint32_t c1 = min(c0 + tile, (uint32_t)w.y + 1);
+                const uint32_t c0 = max((uint32_t)w.x, t * tile);
+                const uint32_t c1 = min((uint32_t)w.y + 1, (t + 1) * tile);
                 const uint32_t ntile = c1 - c0;
-                const uint32_t tile_hi = c1 * d.speclen;
-                // ---- stream postings into the scorecard tile ----
-                // A warp keeps G (peak, bin) lists in flight; each step loads
-                // 128 ids per list with one 16-byte load per lane (the list is
-                // entered at its 16-byte-aligned position; ids before the
-                // cursor or past the list end are masked).
-                // lists are handed out G at a time to whichever warp is free
+                // ---- each (peak, bin) list's postings in this tile: [lb(c0), lb(c1)) ----
+                for (uint32_t pr = tid; pr < np; pr += nthr)
+                {
+                    const uint32_t k = pr / nbin, j = pr - k * nbin;
+                    const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
+                    const uint32_t st = (t == t_first) ? row_lb(col, d.iA, c0, d.speclen) : lend[pr];
+                    const uint32_t en = row_lb(col, d.iA, c1, d.speclen);
+                    lstart[pr] = st;
+                    lend[pr] = en;
+                    loff[pr] = en - st;
+                }
+                __syncthreads();
+                const uint32_t P = block_exclusive_scan(loff, np, T.wsum);
+                if (tid == 0) T.bytes += 4ull * P;
+                HC_PHASE(0);
+                // ---- stream the tile's postings into the scorecard ----
+                // The lists are laid end to end (offsets loff); warps take
+                // chunks of kChunk consecutive postings, so a long list is
+                // spread over all warps. Lane j of a warp describes list ia+j
+                // of a 32-list window; a posting finds its list with a
+                // five-step search over the lanes.
                 for (;;)
                 {
-                    uint32_t base = 0;
-                    if (lane == 0) base = atomicAdd(&T.pnext, (uint32_t)G);
-                    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                    if (base >= np) break;
-                    uint32_t cur[G], end[G], intn[G];
-                    bool live[G];
-#pragma unroll
-                    for (int g = 0; g < G; g++)
+                    uint32_t q0 = 0;
+                    if (lane == 0) q0 = atomicAdd(&T.pnext, kChunk);
+                    q0 = __shfl_sync(0xFFFFFFFFu, q0, 0);
+                    if (q0 >= P) break;
+                    const uint32_t qend = min(q0 + kChunk, P);
+                    uint32_t ia = find_list(loff, np, q0, lane);
+                    uint32_t q = q0;
+                    while (q < qend)
                     {
-                        const uint32_t pr = base + g;
-                        live[g] = pr < np;
-                        cur[g] = live[g] ? pcur[pr] : 0u;
-                        end[g] = live[g] ? pend[pr] : 0u;
-                        intn[g] = live[g] ? pint[pr / nbin] : 0u;
-                        live[g] = live[g] && cur[g] < end[g];
-                    }
-                    for (;;)
-                    {
-                        bool any = false;
-#pragma unroll
-                        for (int g = 0; g < G; g++) any |= live[g];
-                        if (!any) break;
-                        uint4 v[G];
-                        uint32_t a0[G];
-#pragma unroll
-                        for (int g = 0; g < G; g++)
+                        const uint32_t li = ia + (uint32_t)lane;
+                        const uint32_t bend = li < np ? loff[li + 1] : P;            // end of list li
+                        const uint32_t dpos = li < np ? lstart[li] - loff[li] : 0u;  // postings index = offset + dpos
+                        const uint32_t inte = li < np ? pint[li / nbin] : 0u;
+                        const uint32_t hi = min(qend, __shfl_sync(0xFFFFFFFFu, bend, 31));
+                        // the whole window inside list ia: no per-posting search
+                        const bool one = __shfl_sync(0xFFFFFFFFu, bend, 0) >= hi;
+                        for (; q < hi; q += 32u * G)
                         {
-                            a0[g] = cur[g] & ~3u;
-                            const uint32_t p = a0[g] + 4u * lane;
-                            v[g] = (live[g] && p < end[g]) ? ldg4(d.iA + p)
-                                                           : make_uint4(~0u, ~0u, ~0u, ~0u);
-                        }
+                            uint32_t id[G], in[G];
+                            bool ok[G];
 #pragma unroll
-                        for (int g = 0; g < G; g++)
-                        {
-                            if (!live[g]) continue;
-                            const uint32_t ids[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
-                            const uint32_t p0 = a0[g] + 4u * lane;
-                            uint32_t cnt = 0;
-#pragma unroll
-                            for (int j = 0; j < 4; j++)
+                            for (int g = 0; g < G; g++)
                             {
-                                const uint32_t p = p0 + j, id = ids[j];
-                                if (p >= cur[g] && p < end[g] && id < tile_hi)
+                                const uint32_t p = q + 32u * g + (uint32_t)lane;
+                                ok[g] = p < hi;
+                                uint32_t r = 0;
+                                if (!one)
                                 {
-                                    cnt++;
-                                    const uint32_t ppid = __umulhi(id, d.magic) >> d.msh;
-                                    const uint32_t loc = ppid - c0;
-                                    if (loc < ntile)  // below the window (or tile): not a hit here
+#pragma unroll
+                                    for (uint32_t step = 16; step > 0; step >>= 1)
                                     {
-                                        my_inwin++;
-                                        const bool isY = (id - ppid * d.speclen) >= d.half;
-                                        if constexpr (!WIDE)
-                                        {
-                                            // word = [shp:8 | bc:8 | ibc:24 | iyc:24]
-                                            const W add = isY ? ((1ull << 56) | (W)intn[g])
-                                                              : ((1ull << 56) | (1ull << 48) | ((W)intn[g] << 24));
-                                            const W old = atomicAdd(&card[loc], add);
-                                            const uint32_t sh8 = (uint32_t)(old >> 56);
-                                            if (sh8 >= 127u) T.overflow = 1;
-                                            if (sh8 + 1 == a.thr)
-                                            {
-                                                const uint32_t qi = atomicAdd(&T.qcount, 1u);
-                                                if (qi < kQcap) qual[qi] = loc;
-                                            }
-                                        }
-                                        else
-                                        {
-                                            atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)intn[g]);
-                                        }
+                                        const uint32_t bv = __shfl_sync(0xFFFFFFFFu, bend, r + step - 1);
+                                        if (bv <= p) r += step;
                                     }
                                 }
+                                const uint32_t dp = __shfl_sync(0xFFFFFFFFu, dpos, r);
+                                in[g] = __shfl_sync(0xFFFFFFFFu, inte, r);
+                                id[g] = ok[g] ? __ldg(d.iA + (p + dp)) : 0u;
                             }
-                            const uint32_t consumed = __reduce_add_sync(0xFFFFFFFFu, cnt);
-                            const uint32_t chunk_hi = min(end[g], a0[g] + 128u);
-                            const bool whole = consumed == chunk_hi - cur[g];
-                            cur[g] += consumed;
-                            live[g] = whole && cur[g] < end[g];
-                        }
-                    }
-                    if (lane == 0)
-                    {
 #pragma unroll
-                        for (int g = 0; g < G; g++)
-                        {
-                            const uint32_t pr = base + g;
-                            if (pr < np) pcur[pr] = cur[g];
+                            for (int g = 0; g < G; g++)
+                            {
+                                if (!ok[g]) continue;
+                                const uint32_t ppid = __umulhi(id[g], d.magic) >> d.msh;
+                                const uint32_t loc = ppid - c0;
+                                if (loc >= ntile) continue;  // cannot happen: the extents bound the ids
+                                const bool isY = (id[g] - ppid * d.speclen) >= d.half;
+                                if constexpr (!WIDE)
+                                {
+                                    // word = [shp:8 | bc:8 | ibc:24 | iyc:24]
+                                    const W add = isY ? ((1ull << 56) | (W)in[g])
+                                                      : ((1ull << 56) | (1ull << 48) | ((W)in[g] << 24));
+                                    const W old = atomicAdd(&card[loc], add);
+                                    const uint32_t sh8 = (uint32_t)(old >> 56);
+                                    if (sh8 >= 127u) T.overflow = 1;
+                                    if (sh8 + 1 == a.thr)
+                                    {
+                                        const uint32_t qi = atomicAdd(&T.qcount, 1u);
+                                        if (qi < kQcap) qual[qi] = loc;
+                                    }
+                                }
+                                else
+                                {
+                                    atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)in[g]);
+                                }
+                            }
                         }
+                        q = hi;
+                        ia += 32;
                     }
                 }
                 __syncthreads();
@@ -538,9 +586,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                 __syncthreads();
                 HC_PHASE(4);
             }
-            if (my_inwin) atomicAdd(&T.bytes, 4ull * my_inwin);
         }
-        __syncthreads();  // every thread's byte count is in before thread 0 reads it
+        __syncthreads();
         HC_PHASE(5);
         // ---- write the spectrum's results ----
         if (!WIDE && T.overflow)
@@ -898,8 +945,8 @@ uint32_t max_tile(const hc_ctx *ctx, uint32_t dF)
 {
     const size_t extra = smem_layout(0, dF, false).total;
     const size_t room = ctx->smem_optin > extra ? ctx->smem_optin - extra : 0;
-    uint32_t t = (uint32_t)(room / 8) & ~511u;
-    return t < 512 ? 512 : t;
+    const uint32_t t = (uint32_t)(room / 8) / kRowG * kRowG;
+    return t < kRowG ? kRowG : t;
 }
 
 uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm)
@@ -909,8 +956,7 @@ uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm)
     const size_t per = (ctx->smem_optin + 1024) / ctas_per_sm - 1024;
     const size_t extra = smem_layout(0, dF, false).total;
     const size_t room = per > extra ? per - extra : 0;
-    uint32_t t = (uint32_t)(room / 8) & ~511u;
-    return t;
+    return (uint32_t)(room / 8) / kRowG * kRowG;
 }
 
 int prepare_query(hc_ctx *ctx, uint32_t nspec)
@@ -954,6 +1000,27 @@ int launch_search(hc_ctx *ctx, const SearchArgs &a, int grid, uint32_t threads, 
 
 }  // namespace
 
+// the device record of one length
+static void fill_lendev(const hc_ctx *ctx, const LenHost &lh, LenDev &d)
+{
+    std::memset(&d, 0, sizeof(d));
+    d.L = lh.L;
+    d.n = lh.built ? lh.n : 0;
+    d.npep = lh.npep;
+    d.speclen = 2 * ctx->p.maxz * (lh.L - 1);
+    d.half = d.speclen / 2;
+    division_magic(d.speclen, &d.magic, &d.msh);
+    d.stride = lh.stride;
+    d.mass = lh.d_mass;
+    d.seqid = lh.d_seqid;
+    d.sites = lh.d_sites;
+    d.modnum = lh.d_modnum;
+    d.seqs = lh.d_seqs;
+    d.bA = lh.d_bA;
+    d.iA = lh.d_iA;
+    d.rows = lh.d_rows;
+}
+
 int sync_lengths(hc_ctx *ctx)
 {
     if (!ctx->lens_dirty) return HC_SUCCESS;
@@ -961,22 +1028,7 @@ int sync_lengths(hc_ctx *ctx)
     std::vector<LenDev> h(nlen);
     for (uint32_t i = 0; i < nlen; i++)
     {
-        const LenHost &lh = ctx->lens[i];
-        LenDev &d = h[i];
-        std::memset(&d, 0, sizeof(d));
-        d.L = lh.L;
-        d.n = lh.built ? lh.n : 0;
-        d.npep = lh.npep;
-        d.speclen = 2 * ctx->p.maxz * (lh.L - 1);
-        d.half = d.speclen / 2;
-        division_magic(d.speclen, &d.magic, &d.msh);
-        d.mass = lh.d_mass;
-        d.seqid = lh.d_seqid;
-        d.sites = lh.d_sites;
-        d.modnum = lh.d_modnum;
-        d.seqs = lh.d_seqs;
-        d.bA = lh.d_bA;
-        d.iA = lh.d_iA;
+        fill_lendev(ctx, ctx->lens[i], h[i]);
     }
     if (!ctx->d_lens) HC_CUDA(ctx, cudaMalloc((void **)&ctx->d_lens, sizeof(LenDev) * HC_MAX_LENGTHS));
     HC_CUDA(ctx, cudaMemcpy(ctx->d_lens, h.data(), sizeof(LenDev) * nlen, cudaMemcpyHostToDevice));
@@ -1069,7 +1121,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     b.only = q.d_wide;
     b.nonly_dev = q.d_nwide;
     b.work = q.d_work + 1;
-    b.tile = ctx->tuning.tile / 2;
+    b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
     const size_t smem2 = search_smem(b.tile, b.dF, true);
     rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
     if (rc2) return rc2;
@@ -1093,22 +1145,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     LenDev h[HC_MAX_LENGTHS];
     for (uint32_t i = 0; i < nlen; i++)
     {
-        const LenHost &lh = ctx->lens[i];
-        LenDev &d = h[i];
-        std::memset(&d, 0, sizeof(d));
-        d.L = lh.L;
-        d.n = lh.built ? lh.n : 0;
-        d.npep = lh.npep;
-        d.speclen = 2 * ctx->p.maxz * (lh.L - 1);
-        d.half = d.speclen / 2;
-        division_magic(d.speclen, &d.magic, &d.msh);
-        d.mass = lh.d_mass;
-        d.seqid = lh.d_seqid;
-        d.sites = lh.d_sites;
-        d.modnum = lh.d_modnum;
-        d.seqs = lh.d_seqs;
-        d.bA = lh.d_bA;
-        d.iA = lh.d_iA;
+        fill_lendev(ctx, ctx->lens[i], h[i]);
     }
     // pageable source: the copy is staged before the call returns
     HC_CUDA(ctx, cudaMemcpyAsync(s.lens, h, sizeof(LenDev) * nlen, cudaMemcpyHostToDevice, st));
@@ -1161,7 +1198,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     b.only = s.wide;
     b.nonly_dev = nwide;
     b.work = s.work + 1;
-    b.tile = ctx->tuning.tile / 2;
+    b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
     rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true), 2, st);
     if (rc) return rc;
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,

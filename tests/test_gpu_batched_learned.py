@@ -49,7 +49,7 @@ def test_schedules_graph_and_tuner_agree():
     d, args = _dev(q)
     full = ix.tuning()["tile"]
     for t in (dict(schedule=0), dict(schedule=1), dict(schedule=2),
-              dict(schedule=2, ctas_per_sm=2, tile=(full // 2 - 3072) & ~511, threads=256, pairs_per_warp=2)):
+              dict(schedule=2, ctas_per_sm=2, tile=(full // 2 - 4096) // 2048 * 2048, threads=256, pairs_per_warp=2)):
         ix.set_tuning(**t)
         ix.query_device(*args)
         torch.cuda.synchronize()

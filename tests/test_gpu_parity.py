@@ -96,11 +96,11 @@ def test_wide_path(dslim, orc):
 
 
 def test_small_tiles(dslim, orc):
-    """Many scorecard tiles per length (tile smaller than the windows)."""
-    p, db, q = case("mods", 3000, 200, 808)
+    """Many scorecard tiles per length (the smallest tile, windows several tiles wide)."""
+    p, db, q = case("mods", 200000, 100, 808)
     ix = dslim.Index(p)
     ix.construct_all(db)
-    ix.set_tuning(tile=512, threads=256)
+    ix.set_tuning(tile=2048, threads=256)
     res, hist = ix.query(q)
     ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
     compare(res, hist, ores, ohist)
