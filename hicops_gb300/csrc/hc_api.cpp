@@ -134,10 +134,11 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     // default launch shape: one 512-thread CTA per SM, 4 postings lists in
     // flight per warp, the largest scorecard tile the shared memory holds
     ctx->tuning.threads = 512;
-    ctx->tuning.tile = max_tile(ctx, p->dF);
+    ctx->tuning.tile = max_tile(ctx, p->dF, 512);
     ctx->tuning.ctas_per_sm = 1;
     ctx->tuning.pairs_per_warp = 4;
     ctx->tuning.schedule = 0;
+    ctx->tuning.defer_cap = HC_DEFER_MAX;
     *out = ctx;
     return HC_SUCCESS;
 }
@@ -176,10 +177,10 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
     if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < kRowG || (t->tile % kRowG) ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
         (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8) ||
-        t->schedule > 2)
+        t->schedule > 2 || t->defer_cap > HC_DEFER_MAX)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "bad tuning");
-    if (search_smem(t->tile, ctx->p.dF, false) * t->ctas_per_sm > ctx->smem_optin + 1024 * (t->ctas_per_sm - 1) ||
-        search_smem(t->tile, ctx->p.dF, false) > ctx->smem_optin)
+    const size_t need = search_smem(t->tile, ctx->p.dF, false, t->threads);
+    if (need * t->ctas_per_sm > ctx->smem_optin + 1024 * (t->ctas_per_sm - 1) || need > ctx->smem_optin)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "tile does not fit in shared memory");
     ctx->tuning = *t;
     return HC_SUCCESS;

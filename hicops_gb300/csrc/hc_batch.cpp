@@ -78,7 +78,6 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     const hc_tuning saved = ctx->tuning;
-    const uint32_t full = max_tile(ctx, ctx->p.dF);
     std::vector<hc_tuning> cand;
     for (uint32_t sched : {0u, 2u})
         for (uint32_t cps : {1u, 2u})
@@ -91,8 +90,9 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
                     t.pairs_per_warp = g;
                     t.ctas_per_sm = cps;
                     t.schedule = sched;
+                    t.defer_cap = saved.defer_cap;
                     // two resident CTAs share the SM's shared memory
-                    t.tile = cps == 1 ? full : (max_tile_for(ctx, ctx->p.dF, cps));
+                    t.tile = max_tile_for(ctx, ctx->p.dF, cps, thr);
                     if (t.tile < kRowG) continue;
                     cand.push_back(t);
                 }

@@ -166,10 +166,10 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
 int build_row_table(hc_ctx *ctx, LenHost &lh);
 
 // hc_query.cu
-uint32_t max_tile(const hc_ctx *ctx, uint32_t dF);
-uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm);
+uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads);
+uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm, uint32_t threads);
 int prepare_query(hc_ctx *ctx, uint32_t nspec);
-size_t search_smem(uint32_t tile, uint32_t dF, bool wide);
+size_t search_smem(uint32_t tile, uint32_t dF, bool wide, uint32_t threads);
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
                  hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);

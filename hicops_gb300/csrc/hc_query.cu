@@ -36,8 +36,14 @@
 namespace hc {
 namespace {
 
-constexpr int kQcap = 3072;         // qualifying-candidate list per tile
-constexpr uint32_t kChunk = 512;    // postings a warp takes at a time
+// Per-tile shared-memory lists, sized from the tile (tiles are multiples of 2048):
+//   qualifying candidates tile/8 (u32), past which the tile is scored by a full scan;
+//   chunk -> list map tile/4 (u16), past which a chunk finds its list by search.
+__host__ __device__ constexpr uint32_t qual_cap(uint32_t tile) { return tile / 8; }
+__host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 4; }
+constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
+constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
+constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
 constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
@@ -57,6 +63,7 @@ struct SearchArgs
     uint32_t *wide_list, *nwide;
     uint32_t *work;
     uint32_t tile;
+    uint32_t defer_cap;     // <= kDefer
     const uint32_t *only;   // optional list of spectra to process (wide pass)
     const uint32_t *nonly_dev;  // its length, in device memory
     const uint32_t *order;  // optional processing order (longest first)
@@ -109,11 +116,13 @@ struct Card;
 template <>
 struct Card<false>
 {
-    // [shp:8 | bc:8 | ibc:24 | iyc:24] with shp = bc + yc; shp is kept below
-    // 128 (checked per posting), so with intensities < 2^17 the sums stay
-    // below 2^24 and no field can carry into the next.
-    using word = unsigned long long;
-    static constexpr int kWords = 1;
+    // b word [bc:8 | ibc:24] and y word [yc:8 | iyc:24]: a posting is a b or
+    // a y ion, so it adds to one 32-bit word (native shared-memory atomic).
+    // Every atomic returns the word before the add; a count that passes 128
+    // shows as a returned top bit, and the spectrum is redone wide. Below
+    // that, with intensities < 2^17, the sums stay below 2^24.
+    using word = uint32_t;
+    static constexpr int kWords = 2;
 };
 
 template <>
@@ -137,12 +146,13 @@ struct SmemTail
     uint32_t overflow;
     uint32_t spec;
     uint32_t nv;
-    uint32_t pnext;            // next posting (of the tile's lists laid end to end) to hand out
-    uint32_t pad1;
+    uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
+    uint32_t ndefer;           // undecided candidates queued for the exact evaluation
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
-    unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations (pass 1)
+    unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations
+    int2 win[HC_MAX_LENGTHS];  // the spectrum's window per length
     uint32_t wsum[32];         // block scan
     float lgf[kLgTable];
 };
@@ -160,20 +170,22 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, lstart, lend, loff, pmoz, pint, tail, total;
+    size_t qual, cmap, defer, linfo, loff, pmoz, pint, tail, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide)
+__host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide, uint32_t nwarps)
 {
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
     o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
-    o.lstart = o.qual + 4ull * kQcap;
-    o.lend = o.lstart + 4 * maxpairs;
-    o.loff = o.lend + 4 * maxpairs;
+    o.cmap = o.qual + 4ull * qual_cap(tile);
+    o.defer = o.cmap + 2ull * cmap_cap(tile);
+    o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
+    o.loff = o.linfo + 16 * maxpairs;
     o.pmoz = o.loff + 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.tail = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
+    (void)nwarps;
     o.total = o.tail + sizeof(SmemTail);
     return o;
 }
@@ -186,17 +198,25 @@ __device__ __forceinline__ float approx_h(const float *lgf, uint32_t bc, uint32_
     return ((lgf[bc] + lgf[yc]) + log10f(fb)) + log10f(fy) - 6.0f;
 }
 
+__device__ __forceinline__ void decode_packed(uint32_t wb, uint32_t wy, uint32_t &bc, uint32_t &yc, uint32_t &shp,
+                                              uint64_t &ib, uint64_t &iy)
+{
+    bc = wb >> 24;
+    yc = wy >> 24;
+    ib = wb & 0xFFFFFFu;
+    iy = wy & 0xFFFFFFu;
+    shp = (uint32_t)(uint16_t)(bc + yc);
+}
+
 template <bool WIDE>
-__device__ __forceinline__ void decode(const unsigned long long *card, uint32_t loc, uint32_t &bc, uint32_t &yc,
-                                       uint32_t &shp, uint64_t &ib, uint64_t &iy)
+__device__ __forceinline__ void decode(const typename Card<WIDE>::word *card, uint32_t loc, uint32_t &bc,
+                                       uint32_t &yc, uint32_t &shp, uint64_t &ib, uint64_t &iy)
 {
     if constexpr (!WIDE)
     {
-        const unsigned long long wd = card[loc];
-        bc = (uint32_t)(wd >> 48) & 0xFF;
-        yc = (uint32_t)(wd >> 56) - bc;
-        ib = (wd >> 24) & 0xFFFFFF;
-        iy = wd & 0xFFFFFF;
+        const uint2 w = *reinterpret_cast<const uint2 *>(card + 2 * loc);
+        decode_packed(w.x, w.y, bc, yc, shp, ib, iy);
+        return;
     }
     else
     {
@@ -290,6 +310,39 @@ __device__ uint32_t block_exclusive_scan(uint32_t *v, uint32_t n, uint32_t *wsum
     return total;
 }
 
+// One unit of a spectrum's work: the candidates [c0, c1) of length l, at
+// most one scorecard tile (tiles start at multiples of the tile size).
+struct Job
+{
+    uint32_t l, c0, c1;
+};
+
+__device__ __forceinline__ Job job_from(const int2 *win, uint32_t nlen, uint32_t tile, uint32_t l)
+{
+    for (; l < nlen; l++)
+    {
+        const int2 w = win[l];
+        if (w.x <= w.y)
+        {
+            const uint32_t c0 = (uint32_t)w.x;
+            return Job{l, c0, min((uint32_t)w.y + 1, (c0 / tile + 1) * tile)};
+        }
+    }
+    return Job{kNoJob, 0u, 0u};
+}
+
+__device__ __forceinline__ Job first_job(const int2 *win, uint32_t nlen, uint32_t tile)
+{
+    return job_from(win, nlen, tile, 0);
+}
+
+__device__ __forceinline__ Job next_job(const Job &j, const int2 *win, uint32_t nlen, uint32_t tile)
+{
+    const uint32_t end = (uint32_t)win[j.l].y + 1;
+    if (j.c1 < end) return Job{j.l, j.c1, min(end, j.c1 + tile)};
+    return job_from(win, nlen, tile, j.l + 1);
+}
+
 // The last list i in [0, n) with off[i] <= q (off ascending, off[0] = 0):
 // a 32-way search, one shared-memory read per lane per round.
 __device__ __forceinline__ uint32_t find_list(const uint32_t *off, uint32_t n, uint32_t q, int lane)
@@ -307,21 +360,23 @@ __device__ __forceinline__ uint32_t find_list(const uint32_t *off, uint32_t n, u
 }
 
 template <bool WIDE, int G>
-__global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
+__global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(SearchArgs a)
 {
     using W = typename Card<WIDE>::word;
     constexpr int NW = Card<WIDE>::kWords;
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t tile = a.tile;
     const uint32_t nbin = 2 * a.dF + 1;
-    const SmemLayout L = smem_layout(tile, a.dF, WIDE);
+    const SmemLayout L = smem_layout(tile, a.dF, WIDE, blockDim.x >> 5);
     W *card = reinterpret_cast<W *>(smem);
     uint32_t *qual = reinterpret_cast<uint32_t *>(smem + L.qual);
-    uint32_t *lstart = reinterpret_cast<uint32_t *>(smem + L.lstart);
-    uint32_t *lend = reinterpret_cast<uint32_t *>(smem + L.lend);
+    uint2 *defer = reinterpret_cast<uint2 *>(smem + L.defer);  // undecided candidates: {b word, y word}
+    uint4 *linfo = reinterpret_cast<uint4 *>(smem + L.linfo);  // per list: {first, end, chunk offset, intensity}
     uint32_t *loff = reinterpret_cast<uint32_t *>(smem + L.loff);
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
+    uint16_t *cmap = reinterpret_cast<uint16_t *>(smem + L.cmap);    // chunk -> list
+    const uint32_t qcap = qual_cap(tile), ccap = cmap_cap(tile);
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
 
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -360,11 +415,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
             T.maxbits = 0;
             T.cpsms = 0;
             T.qcount = 0;
+            T.ndefer = 0;
             T.flags = WIDE ? HC_FLAG_WIDE : 0u;
             T.overflow = 0;
             T.bytes = 0;
             T.nv = 0;
         }
+        for (uint32_t l = tid; l < a.nlen; l += nthr) T.win[l] = a.win[(size_t)s * a.nlen + l];
         __syncthreads();
         // valid peaks (dslim_query.cpp:625): dF < qion < max*scale - 1 - dF
         {
@@ -390,134 +447,202 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
         const uint32_t np = nv * nbin;
         unsigned long long my_best = 0;
         uint32_t my_shp = 0;
+        if (tid == 0)
+            for (uint32_t l = 0; l < a.nlen; l++)
+                if (T.win[l].x <= T.win[l].y) T.bytes += 4ull * (2 * a.dF + 2) * nv;  // the reference's bA reads
 
-        for (uint32_t l = 0; l < a.nlen; l++)
+        // The spectrum's work is a sequence of jobs (length l, scorecard tile
+        // t). Tiles are aligned to multiples of the tile size, so interior
+        // tile boundaries are row-table entries; only a window's own ends need
+        // a search inside one row. While job j streams, every thread already
+        // has the row-table words of job j+1's boundaries in flight.
+        Job jb = first_job(T.win, a.nlen, tile);
+        uint32_t pf_lo[kPf], pf_hi[kPf], ps_lo[kPf], ps_hi[kPf];
+        if (jb.l != kNoJob)
         {
-            const int2 w = a.win[(size_t)s * a.nlen + l];
-            if (w.x > w.y) continue;
-            const LenDev d = a.lens[l];
-            // bA reads of the reference: two per (peak, bin), one more per peak
-            if (tid == 0) T.bytes += 4ull * (2 * a.dF + 2) * nv;
-            // tiles are aligned to multiples of the tile size, so their
-            // interior boundaries are row-table entries; only the window's
-            // own ends are searched (inside one row)
-            const uint32_t t_first = (uint32_t)w.x / tile, t_last = (uint32_t)w.y / tile;
-            for (uint32_t t = t_first; t <= t_last; t++)
+            // the first job's boundaries, directly
+            const LenDev d = a.lens[jb.l];
+            for (uint32_t pr = tid; pr < np; pr += nthr)
             {
-                const uint32_t c0 = max((uint32_t)w.x, t * tile);
-                const uint32_t c1 = min((uint32_t)w.y + 1, (t + 1) * tile);
-                const uint32_t ntile = c1 - c0;
-                // ---- each (peak, bin) list's postings in this tile: [lb(c0), lb(c1)) ----
+                const uint32_t k = pr / nbin, j = pr - k * nbin;
+                const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
+                const uint32_t st = row_lb(col, d.iA, jb.c0, d.speclen);
+                const uint32_t en = row_lb(col, d.iA, jb.c1, d.speclen);
+                linfo[pr] = make_uint4(st, en, 0u, pint[k]);
+                loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+            }
+        }
+        uint32_t C = 0;
+        while (jb.l != kNoJob)
+        {
+            const LenDev d = a.lens[jb.l];
+            const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
+            // ---- chunk offsets of this job's lists ----
+            // A list is read in 16-byte chunks (4 postings) from its first
+            // posting rounded down to a multiple of 4; the chunks of all
+            // lists are numbered end to end (offsets loff).
+            {
+                uint32_t my_post = 0;
+                for (uint32_t pr = tid; pr < np; pr += nthr) my_post += linfo[pr].y - linfo[pr].x;
+                my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
+                if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);
+                __syncthreads();
+                C = block_exclusive_scan(loff, np, T.wsum);
                 for (uint32_t pr = tid; pr < np; pr += nthr)
                 {
-                    const uint32_t k = pr / nbin, j = pr - k * nbin;
-                    const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
-                    const uint32_t st = (t == t_first) ? row_lb(col, d.iA, c0, d.speclen) : lend[pr];
-                    const uint32_t en = row_lb(col, d.iA, c1, d.speclen);
-                    lstart[pr] = st;
-                    lend[pr] = en;
-                    loff[pr] = en - st;
+                    const uint32_t k0 = loff[pr], k1 = min(loff[pr + 1], ccap);
+                    linfo[pr].z = k0;
+                    for (uint32_t k = k0; k < k1; k++) cmap[k] = (uint16_t)pr;
                 }
                 __syncthreads();
-                const uint32_t P = block_exclusive_scan(loff, np, T.wsum);
-                if (tid == 0) T.bytes += 4ull * P;
-                HC_PHASE(0);
-                // ---- stream the tile's postings into the scorecard ----
-                // The lists are laid end to end (offsets loff); warps take
-                // chunks of kChunk consecutive postings, so a long list is
-                // spread over all warps. Lane j of a warp describes list ia+j
-                // of a 32-list window; a posting finds its list with a
-                // five-step search over the lanes.
-                for (;;)
+            }
+            HC_PHASE(0);
+            // ---- row-table words of the next job's boundaries, in flight ----
+            const Job nj = next_job(jb, T.win, a.nlen, tile);
+            const bool same = nj.l == jb.l;
+            LenDev dn;
+            if (nj.l != kNoJob)
+            {
+                dn = same ? d : a.lens[nj.l];
+#pragma unroll
+                for (int m = 0; m < kPf; m++)
                 {
-                    uint32_t q0 = 0;
-                    if (lane == 0) q0 = atomicAdd(&T.pnext, kChunk);
-                    q0 = __shfl_sync(0xFFFFFFFFu, q0, 0);
-                    if (q0 >= P) break;
-                    const uint32_t qend = min(q0 + kChunk, P);
-                    uint32_t ia = find_list(loff, np, q0, lane);
-                    uint32_t q = q0;
-                    while (q < qend)
+                    const uint32_t pr = tid + m * nthr;
+                    if (pr < np)
                     {
-                        const uint32_t li = ia + (uint32_t)lane;
-                        const uint32_t bend = li < np ? loff[li + 1] : P;            // end of list li
-                        const uint32_t dpos = li < np ? lstart[li] - loff[li] : 0u;  // postings index = offset + dpos
-                        const uint32_t inte = li < np ? pint[li / nbin] : 0u;
-                        const uint32_t hi = min(qend, __shfl_sync(0xFFFFFFFFu, bend, 31));
-                        // the whole window inside list ia: no per-posting search
-                        const bool one = __shfl_sync(0xFFFFFFFFu, bend, 0) >= hi;
-                        for (; q < hi; q += 32u * G)
+                        const uint32_t k = pr / nbin, j = pr - k * nbin;
+                        const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
+                        const uint32_t ke = nj.c1 / kRowG;
+                        pf_lo[m] = __ldg(col + ke);
+                        pf_hi[m] = (nj.c1 == ke * kRowG) ? 0u : __ldg(col + ke + 1);
+                        if (!same)
                         {
-                            uint32_t id[G], in[G];
-                            bool ok[G];
-#pragma unroll
-                            for (int g = 0; g < G; g++)
-                            {
-                                const uint32_t p = q + 32u * g + (uint32_t)lane;
-                                ok[g] = p < hi;
-                                uint32_t r = 0;
-                                if (!one)
-                                {
-#pragma unroll
-                                    for (uint32_t step = 16; step > 0; step >>= 1)
-                                    {
-                                        const uint32_t bv = __shfl_sync(0xFFFFFFFFu, bend, r + step - 1);
-                                        if (bv <= p) r += step;
-                                    }
-                                }
-                                const uint32_t dp = __shfl_sync(0xFFFFFFFFu, dpos, r);
-                                in[g] = __shfl_sync(0xFFFFFFFFu, inte, r);
-                                id[g] = ok[g] ? __ldg(d.iA + (p + dp)) : 0u;
-                            }
-#pragma unroll
-                            for (int g = 0; g < G; g++)
-                            {
-                                if (!ok[g]) continue;
-                                const uint32_t ppid = __umulhi(id[g], d.magic) >> d.msh;
-                                const uint32_t loc = ppid - c0;
-                                if (loc >= ntile) continue;  // cannot happen: the extents bound the ids
-                                const bool isY = (id[g] - ppid * d.speclen) >= d.half;
-                                if constexpr (!WIDE)
-                                {
-                                    // word = [shp:8 | bc:8 | ibc:24 | iyc:24]
-                                    const W add = isY ? ((1ull << 56) | (W)in[g])
-                                                      : ((1ull << 56) | (1ull << 48) | ((W)in[g] << 24));
-                                    const W old = atomicAdd(&card[loc], add);
-                                    const uint32_t sh8 = (uint32_t)(old >> 56);
-                                    if (sh8 >= 127u) T.overflow = 1;
-                                    if (sh8 + 1 == a.thr)
-                                    {
-                                        const uint32_t qi = atomicAdd(&T.qcount, 1u);
-                                        if (qi < kQcap) qual[qi] = loc;
-                                    }
-                                }
-                                else
-                                {
-                                    atomicAdd(&card[2 * loc + (isY ? 1 : 0)], (1ull << 40) | (W)in[g]);
-                                }
-                            }
+                            const uint32_t ks = nj.c0 / kRowG;
+                            ps_lo[m] = __ldg(col + ks);
+                            ps_hi[m] = (nj.c0 == ks * kRowG) ? 0u : __ldg(col + ks + 1);
                         }
-                        q = hi;
-                        ia += 32;
                     }
                 }
-                __syncthreads();
-                HC_PHASE(1);
-                // ---- score the candidates that reached min_shp ----
-                // pass 1: hyperscore (float, exact where the bound leaves the
-                // sign or the bin open), cpsms, histogram, tile maximum
-                const uint32_t qn = T.qcount;
-                const bool scan_all = WIDE || qn > (uint32_t)kQcap || a.thr > 250;
-                const uint32_t nscore = scan_all ? (c1 - c0) : qn;
-                uint32_t my_exact = 0;
-                if (a.phase && tid == 0)
+            }
+            // ---- stream the job's postings into the scorecard ----
+            // A warp takes 32*G consecutive chunks; lane j handles chunks
+            // q0 + j + 32g. All G loads are issued before any is used.
+            uint32_t ovf = 0;  // OR of the words the atomics returned
+            for (;;)
+            {
+                uint32_t q0 = 0;
+                if (lane == 0) q0 = atomicAdd(&T.pnext, 32u * G);
+                q0 = __shfl_sync(0xFFFFFFFFu, q0, 0);
+                if (q0 >= C) break;
+                uint4 v[G];
+                uint32_t rel[G], span[G], inte[G];  // chunk start - list start, list length, intensity
+#pragma unroll
+                for (int g = 0; g < G; g++)
                 {
-                    T.cnt[0] += 1;
-                    T.cnt[1] += scan_all ? 1 : 0;
-                    T.cnt[2] += qn;
+                    const uint32_t kb = q0 + 32u * g;
+                    const uint32_t kc = kb + (uint32_t)lane;
+                    rel[g] = 0u;
+                    span[g] = 0u;  // no chunk: every posting fails the range test
+                    inte[g] = 0u;
+                    v[g] = make_uint4(0u, 0u, 0u, 0u);
+                    if (kb < C)  // warp-uniform
+                    {
+                        uint32_t i = 0;
+                        if (kb + 32u > ccap)  // past the map: search
+                            i = find_list(loff, np, kb, lane);
+                        if (kc < C)
+                        {
+                            if (kc < ccap) i = cmap[kc];
+                            else
+                                while (i + 1 < np && loff[i + 1] <= kc) i++;
+                            const uint4 li = linfo[i];
+                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - li.z);
+                            rel[g] = pos - li.x;  // wraps below zero for the leading padding
+                            span[g] = li.y - li.x;
+                            inte[g] = li.w;
+                            v[g] = __ldg(reinterpret_cast<const uint4 *>(d.iA + pos));
+                        }
+                    }
                 }
+#pragma unroll
+                for (int g = 0; g < G; g++)
+                {
+                    const uint32_t ids[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
+                    uint32_t loc[4];
+                    W add[4];
+                    bool ok[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++)
+                    {
+                        const uint32_t ppid = __umulhi(ids[e], d.magic) >> d.msh;
+                        loc[e] = ppid - c0;
+                        ok[e] = (rel[g] + (uint32_t)e) < span[g] && loc[e] < ntile;
+                        const bool isY = (ids[e] - ppid * d.speclen) >= d.half;
+                        loc[e] = 2 * loc[e] + (isY ? 1u : 0u);
+                        if constexpr (!WIDE)
+                            add[e] = (1u << 24) | inte[g];
+                        else
+                            add[e] = (1ull << 40) | (W)inte[g];
+                    }
+                    if constexpr (!WIDE)
+                    {
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if (ok[e]) ovf |= atomicAdd(&card[loc[e]], add[e]);
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if (ok[e]) atomicAdd(&card[loc[e]], add[e]);
+                    }
+                }
+            }
+            if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
+            __syncthreads();
+            HC_PHASE(1);
+            // ---- list the candidates that reached min_shp ----
+            // two candidates (four words, 16 bytes) per lane and step; a warp
+            // appends its qualifying candidates with one counter atomic
+            if constexpr (!WIDE)
+            {
+                const uint4 *c4 = reinterpret_cast<const uint4 *>(card);
+                for (uint32_t base = 2 * (tid - (uint32_t)lane); base < ntile; base += 2 * nthr)
+                {
+                    const uint32_t c = base + 2 * (uint32_t)lane;
+                    // words past ntile are zero (the tile is cleared after use)
+                    const uint4 w = c < ntile ? c4[c >> 1] : make_uint4(0u, 0u, 0u, 0u);
+                    const uint32_t s0 = (w.x >> 24) + (w.y >> 24), s1 = (w.z >> 24) + (w.w >> 24);
+                    const bool q0 = s0 >= a.min_shp && s0 != 0, q1 = s1 >= a.min_shp && s1 != 0;
+                    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, q0), b1 = __ballot_sync(0xFFFFFFFFu, q1);
+                    if ((b0 | b1) == 0) continue;
+                    const uint32_t lt = (1u << lane) - 1u;
+                    uint32_t qb = 0;
+                    if (lane == 0) qb = atomicAdd(&T.qcount, (uint32_t)(__popc(b0) + __popc(b1)));
+                    qb = __shfl_sync(0xFFFFFFFFu, qb, 0);
+                    uint32_t qi = qb + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
+                    if (q0 && qi < qcap) qual[qi] = c;
+                    qi += q0 ? 1u : 0u;
+                    if (q1 && qi < qcap) qual[qi] = c + 1;
+                }
+                __syncthreads();
+            }
+            const uint32_t qn = T.qcount;
+            const bool scan_all = WIDE || qn > qcap;
+            const uint32_t nscore = scan_all ? ntile : qn;
+            if (a.phase && tid == 0)
+            {
+                T.cnt[0] += 1;
+                T.cnt[1] += scan_all ? 1 : 0;
+                T.cnt[2] += qn;
+            }
+            // pass 1: cpsms, histogram and tile maximum from the float
+            // estimate; candidates whose sign or bin the estimate leaves open
+            // are queued (their two words) and resolved exactly once the
+            // spectrum is done
+            {
                 float my_max = 0.0f;
-                uint32_t my_cps = 0, my_fl = 0;
+                uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
                 for (uint32_t i = tid; i < nscore; i += nthr)
                 {
                     const uint32_t loc = scan_all ? i : qual[i];
@@ -527,65 +652,165 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024) k_search(SearchArgs a)
                     if (shp < a.min_shp || shp == 0) continue;
                     float h;
                     int bin;
-                    if (!score<WIDE>(a.qc, T.lgf, bc, yc, ib, iy, h, bin, my_exact)) continue;
+                    if constexpr (!WIDE)
+                    {
+                        const float ha = approx_h(T.lgf, bc, yc, ib, iy);
+                        const float tt = ha * 10.0f + 0.5f;
+                        const float fr = tt - floorf(tt);
+                        if (fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin)
+                        {
+                            if (ha > 0.0f) my_max = fmaxf(my_max, ha);
+                            const uint32_t di = atomicAdd(&T.ndefer, 1u);
+                            if (di < a.defer_cap)
+                            {
+                                defer[di] = make_uint2((uint32_t)ib | (bc << 24), (uint32_t)iy | (yc << 24));
+                                continue;
+                            }
+                            my_exact++;  // queue full: exact now
+                            h = exact_h(a.qc, bc, yc, ib, iy);
+                            bin = hist_bin(h);
+                            if (!(h > 0.0f)) continue;
+                        }
+                        else
+                        {
+                            if (!(ha > 0.0f)) continue;
+                            h = ha;
+                            bin = (int)floorf(tt);
+                        }
+                    }
+                    else
+                    {
+                        my_exact++;
+                        h = exact_h(a.qc, bc, yc, ib, iy);
+                        bin = hist_bin(h);
+                        if (!(h > 0.0f)) continue;
+                    }
                     my_cps++;
                     if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
                     if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
                     atomicAdd(&T.hist[bin], 1u);
                     my_max = fmaxf(my_max, h);
                 }
-                if (my_cps) atomicAdd(&T.cpsms, my_cps);
+                my_cps = __reduce_add_sync(0xFFFFFFFFu, my_cps);
+                my_fl = __reduce_or_sync(0xFFFFFFFFu, my_fl);
+                const uint32_t mb = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(my_max));  // my_max >= 0
+                if (lane == 0)
+                {
+                    if (my_cps) atomicAdd(&T.cpsms, my_cps);
+                    if (my_fl) atomicOr(&T.flags, my_fl);
+                    if (mb) atomicMax(&T.maxbits, mb);
+                }
                 if (a.phase && my_exact) atomicAdd(&T.cnt[3], (unsigned long long)my_exact);
-                if (my_fl) atomicOr(&T.flags, my_fl);
-                if (my_max > 0.0f) atomicMax(&T.maxbits, __float_as_uint(my_max));
-                __syncthreads();
-                HC_PHASE(2);
-                // pass 2: the reference's double hyperscore for every candidate
-                // that can still be the top hit (within kNear of the maximum so far)
-                {
-                    const float runmax = __uint_as_float(T.maxbits);
-                    if (runmax > 0.0f)
-                        for (uint32_t i = tid; i < nscore; i += nthr)
-                        {
-                            const uint32_t loc = scan_all ? i : qual[i];
-                            uint32_t bc, yc, shp;
-                            uint64_t ib, iy;
-                            decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
-                            if (shp < a.min_shp || shp == 0) continue;
-                            const float ha = WIDE ? exact_h(a.qc, bc, yc, ib, iy) : approx_h(T.lgf, bc, yc, ib, iy);
-                            if (ha < runmax - kNear) continue;
-                            const float he = WIDE ? ha : exact_h(a.qc, bc, yc, ib, iy);
-                            if (!(he > 0.0f)) continue;
-                            const uint32_t psid = c0 + loc;
-                            const uint32_t tie = (l << 24) | (psid & 0xFFFFFF);
-                            const unsigned long long key =
-                                ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
-                            if (key > my_best)
-                            {
-                                my_best = key;
-                                my_shp = shp;
-                            }
-                            atomicMax(&T.best, key);
-                        }
-                }
-                __syncthreads();
-                HC_PHASE(3);
-                if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
-                // ---- clear the tile ----
-                {
-                    const uint32_t nw = (c1 - c0) * NW;
-                    uint4 *c4 = reinterpret_cast<uint4 *>(card);
-                    const uint32_t n4 = (nw + 1) / 2;
-                    for (uint32_t i = tid; i < n4; i += nthr) c4[i] = make_uint4(0, 0, 0, 0);
-                }
-                if (tid == 0)
-                {
-                    T.qcount = 0;
-                    T.pnext = 0;
-                }
-                __syncthreads();
-                HC_PHASE(4);
             }
+            __syncthreads();
+            HC_PHASE(2);
+            // pass 2: the reference's double hyperscore for every candidate
+            // that can still be the top hit (within kNear of the maximum so far)
+            {
+                const float runmax = __uint_as_float(T.maxbits);
+                if (runmax > 0.0f)
+                    for (uint32_t i = tid; i < nscore; i += nthr)
+                    {
+                        const uint32_t loc = scan_all ? i : qual[i];
+                        uint32_t bc, yc, shp;
+                        uint64_t ib, iy;
+                        decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
+                        if (shp < a.min_shp || shp == 0) continue;
+                        const float ha = WIDE ? exact_h(a.qc, bc, yc, ib, iy) : approx_h(T.lgf, bc, yc, ib, iy);
+                        if (ha < runmax - kNear) continue;
+                        const float he = WIDE ? ha : exact_h(a.qc, bc, yc, ib, iy);
+                        if (!(he > 0.0f)) continue;
+                        const uint32_t psid = c0 + loc;
+                        const uint32_t tie = (jb.l << 24) | (psid & 0xFFFFFF);
+                        const unsigned long long key =
+                            ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
+                        if (key > my_best)
+                        {
+                            my_best = key;
+                            my_shp = shp;
+                        }
+                        atomicMax(&T.best, key);
+                    }
+            }
+            __syncthreads();
+            HC_PHASE(3);
+            if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
+            // ---- clear the tile ----
+            {
+                uint4 *c4 = reinterpret_cast<uint4 *>(card);
+                const uint32_t n4 = (uint32_t)(((size_t)ntile * NW * sizeof(W) + 15) / 16);
+                for (uint32_t i = tid; i < n4; i += nthr) c4[i] = make_uint4(0, 0, 0, 0);
+            }
+            if (tid == 0)
+            {
+                T.qcount = 0;
+                T.pnext = 0;
+            }
+            // ---- the next job's list bounds from the prefetched words ----
+            // (each thread rewrites only its own lists; the stream that read
+            // linfo/loff ended at the barrier above)
+            if (nj.l != kNoJob)
+            {
+#pragma unroll
+                for (int m = 0; m < kPf; m++)
+                {
+                    const uint32_t pr = tid + m * nthr;
+                    if (pr < np)
+                    {
+                        const uint32_t st = same ? linfo[pr].y
+                                                 : (nj.c0 % kRowG == 0u
+                                                        ? ps_lo[m]
+                                                        : lower_bound_g(dn.iA, ps_lo[m], ps_hi[m], nj.c0 * dn.speclen));
+                        const uint32_t en = (nj.c1 % kRowG == 0u)
+                                                ? pf_lo[m]
+                                                : lower_bound_g(dn.iA, pf_lo[m], pf_hi[m], nj.c1 * dn.speclen);
+                        linfo[pr] = make_uint4(st, en, 0u, pint[pr / nbin]);
+                        loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                    }
+                }
+                // lists past kPf * nthr (small blocks, wide bin windows): directly
+                for (uint32_t pr = tid + kPf * nthr; pr < np; pr += nthr)
+                {
+                    const uint32_t k = pr / nbin, j = pr - k * nbin;
+                    const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
+                    const uint32_t st = same ? linfo[pr].y : row_lb(col, dn.iA, nj.c0, dn.speclen);
+                    const uint32_t en = row_lb(col, dn.iA, nj.c1, dn.speclen);
+                    linfo[pr] = make_uint4(st, en, 0u, pint[k]);
+                    loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                }
+            }
+            __syncthreads();
+            HC_PHASE(4);
+            jb = nj;
+        }
+        // ---- candidates whose sign or bin the float estimate left open ----
+        if (!WIDE)
+        {
+            const uint32_t nd = min(T.ndefer, a.defer_cap);
+            uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
+            for (uint32_t i = tid; i < nd; i += nthr)
+            {
+                uint32_t bc, yc, shp;
+                uint64_t ib, iy;
+                const uint2 w = defer[i];
+                decode_packed(w.x, w.y, bc, yc, shp, ib, iy);
+                my_exact++;
+                const float h = exact_h(a.qc, bc, yc, ib, iy);
+                if (!(h > 0.0f)) continue;
+                int bin = hist_bin(h);
+                my_cps++;
+                if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
+                if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
+                atomicAdd(&T.hist[bin], 1u);
+            }
+            my_cps = __reduce_add_sync(0xFFFFFFFFu, my_cps);
+            my_fl = __reduce_or_sync(0xFFFFFFFFu, my_fl);
+            if (lane == 0)
+            {
+                if (my_cps) atomicAdd(&T.cpsms, my_cps);
+                if (my_fl) atomicOr(&T.flags, my_fl);
+            }
+            if (a.phase && my_exact) atomicAdd(&T.cnt[3], (unsigned long long)my_exact);
         }
         __syncthreads();
         HC_PHASE(5);
@@ -936,27 +1161,34 @@ __global__ void k_order(const uint32_t *__restrict__ cls, uint32_t nspec, const 
 
 }  // namespace
 
-size_t search_smem(uint32_t tile, uint32_t dF, bool wide) { return smem_layout(tile, dF, wide).total; }
+size_t search_smem(uint32_t tile, uint32_t dF, bool wide, uint32_t threads)
+{
+    return smem_layout(tile, dF, wide, threads / 32).total;
+}
 
 template <class T>
 static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need);
 
-uint32_t max_tile(const hc_ctx *ctx, uint32_t dF)
+// the largest tile (a multiple of kRowG) whose whole layout fits in `budget` bytes
+static uint32_t fit_tile(size_t budget, uint32_t dF, uint32_t threads)
 {
-    const size_t extra = smem_layout(0, dF, false).total;
-    const size_t room = ctx->smem_optin > extra ? ctx->smem_optin - extra : 0;
-    const uint32_t t = (uint32_t)(room / 8) / kRowG * kRowG;
+    uint32_t t = (uint32_t)std::min<size_t>(budget / 8, 1u << 24) / kRowG * kRowG;
+    while (t > kRowG && smem_layout(t, dF, false, threads / 32).total > budget) t -= kRowG;
     return t < kRowG ? kRowG : t;
 }
 
-uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm)
+uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads)
 {
-    if (ctas_per_sm <= 1) return max_tile(ctx, dF);
+    return fit_tile(ctx->smem_optin, dF, threads);
+}
+
+uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm, uint32_t threads)
+{
+    if (ctas_per_sm <= 1) return max_tile(ctx, dF, threads);
     // the SM's shared memory (optin + 1 KB) is split; each CTA keeps 1 KB for the system
     const size_t per = (ctx->smem_optin + 1024) / ctas_per_sm - 1024;
-    const size_t extra = smem_layout(0, dF, false).total;
-    const size_t room = per > extra ? per - extra : 0;
-    return (uint32_t)(room / 8) / kRowG * kRowG;
+    const uint32_t t = fit_tile(per, dF, threads);
+    return smem_layout(t, dF, false, threads / 32).total <= per ? t : 0u;
 }
 
 int prepare_query(hc_ctx *ctx, uint32_t nspec)
@@ -1094,6 +1326,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.nwide = q.d_nwide;
     a.work = q.d_work;
     a.tile = ctx->tuning.tile;
+    a.defer_cap = ctx->tuning.defer_cap;
     a.persistent = sched != 1;
     a.phase = ctx->d_phase;
     int launches = 4;
@@ -1106,7 +1339,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
         a.order = q.d_order;
         launches += 2;
     }
-    const size_t smem = search_smem(a.tile, a.dF, false);
+    const size_t smem = search_smem(a.tile, a.dF, false, ctx->tuning.threads);
     const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     int rc2 = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
@@ -1122,7 +1355,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     b.nonly_dev = q.d_nwide;
     b.work = q.d_work + 1;
     b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
-    const size_t smem2 = search_smem(b.tile, b.dF, true);
+    const size_t smem2 = search_smem(b.tile, b.dF, true, ctx->tuning.threads);
     rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
     if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
@@ -1176,6 +1409,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     a.nwide = nwide;
     a.work = s.work;
     a.tile = ctx->tuning.tile;
+    a.defer_cap = ctx->tuning.defer_cap;
     const uint32_t sched = ctx->tuning.schedule;
     a.persistent = sched != 1;
     int launches = 4;
@@ -1188,7 +1422,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
         a.order = s.order;
         launches += 2;
     }
-    const size_t smem = search_smem(a.tile, a.dF, false);
+    const size_t smem = search_smem(a.tile, a.dF, false, ctx->tuning.threads);
     const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
     int rc = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
     if (rc) return rc;
@@ -1199,7 +1433,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     b.nonly_dev = nwide;
     b.work = s.work + 1;
     b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
-    rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true), 2, st);
+    rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true, ctx->tuning.threads), 2, st);
     if (rc) return rc;
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
                                                                             ctx->p.expect_max, s.fitstart);

@@ -318,6 +318,9 @@ def workload(name: str):
     if name == "open-200k":       # open-2m's shape at 1/10 of the database, 5,000 spectra (profiling)
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 200000, 0xC12, 5000, 0xC13, {}
+    if name == "open-500k":       # open-2m's shape at 1/4 of the database, 2,000 spectra (kernel profiles)
+        p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+        return p, 500000, 0xC14, 2000, 0xC15, {}
     if name == "mixed-2m":        # open-2m index, 200k spectra, 20-150 peaks, mixed windows
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 2000000, 0xC10, 200000, 0xC21, dict(

@@ -109,11 +109,17 @@ typedef struct hc_tuning
     uint32_t threads;      /* threads per CTA (multiple of 32, <= 1024) */
     uint32_t tile;         /* scorecard candidates per shared-memory tile */
     uint32_t ctas_per_sm;  /* resident CTAs per SM the grid is sized for */
-    uint32_t pairs_per_warp; /* (peak, bin) postings lists a warp streams at once */
+    uint32_t pairs_per_warp; /* 16-byte postings chunks (4 postings each) a lane keeps
+                                in flight: 1, 2, 4 or 8 */
     uint32_t schedule;     /* 0: persistent CTAs, work stealing in batch order;
                               1: plain, one CTA per spectrum;
                               2: batched, persistent CTAs, longest windows first */
+    uint32_t defer_cap;    /* candidates per spectrum whose hyperscore sign or histogram
+                              bin the float estimate leaves open, queued for one exact
+                              evaluation at the spectrum's end (<= HC_DEFER_MAX; 0: each
+                              is evaluated in place). Results do not depend on it. */
 } hc_tuning;
+#define HC_DEFER_MAX 256
 
 int hc_version(void);
 const char *hc_status_string(int status);

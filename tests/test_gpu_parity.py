@@ -107,6 +107,35 @@ def test_small_tiles(dslim, orc):
     ix.close()
 
 
+@pytest.mark.parametrize("threads,ppw", [(64, 1), (128, 2)])
+def test_small_blocks(dslim, orc, threads, ppw):
+    """Blocks smaller than a third of the (peak, bin) lists: list bounds past
+    the per-thread prefetch slots are computed directly."""
+    p, db, q = case("mods", 20000, 120, 818)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    ix.set_tuning(tile=4096, threads=threads, pairs_per_warp=ppw, ctas_per_sm=1)
+    res, hist = ix.query(q)
+    ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
+@pytest.mark.parametrize("cap", [0, 1, 256])
+def test_undecided_queue_capacity(dslim, orc, cap):
+    """Candidates whose sign or histogram bin the float estimate leaves open:
+    evaluated in place (cap 0), mostly in place once a one-entry queue is full,
+    or queued and resolved at the spectrum's end; all give the oracle's results."""
+    p, db, q = case("mods", 20000, 150, 828)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    ix.set_tuning(defer_cap=cap)
+    res, hist = ix.query(q)
+    ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
 def test_empty_and_edge_batches(dslim, orc):
     p, db, q = case("plain", 1000, 50, 909)
     ix = dslim.Index(p)
