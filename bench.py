@@ -2,11 +2,20 @@
 
 One step = one search of the whole query batch (100,000 spectra, 100 peaks,
 dF 0.01 Da, dM +-500 Da, fragment charges 1-3) against the device-resident
-index of 2,000,000 synthetic tryptic peptides with variable M-oxidation (<= 2).
-`value` is spectra/s with the batch resident in HBM; `e2e` is the same through
-the host-buffer C-ABI call (pinned inputs copied in, results copied out).
-The index (~2 GB of postings) is far larger than L2, so no L2 flush is needed
-between steps.
+index of 2,000,000 synthetic tryptic peptides with variable M-oxidation (<= 2),
+followed by the e-values.
+
+Two forms run on the same batch and must give the same PSMs:
+  plain            one CTA per spectrum, default launch shape, separate launches,
+                   expeRT tail-fit e-values;
+  batched+learned  the autotuned persistent kernel (longest windows first,
+                   work stealing) replayed from a CUDA graph, then the learned
+                   e-value tail (MLP trained here on the plain run's histograms,
+                   expeRT as fallback and judge).
+`value` is the batched+learned spectra/s with the batch resident in HBM; the
+plain form's numbers sit beside it. `e2e` is the host-buffer C-ABI call
+(hc_dslim_query: pinned inputs copied in, results copied out). The index is
+far larger than L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -46,16 +55,6 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
-
-
-def traffic_per_spectrum():
-    """DRAM bytes per spectrum of the search kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_search_traffic.json")
-    if os.path.exists(path):
-        with open(path) as f:
-            d = json.load(f)
-        return float(d["dram_bytes_per_spectrum"])
-    return None
 
 
 class Clocks:
@@ -173,6 +172,15 @@ def run_reference(args, rank, world, dist):
     print(json.dumps(out), flush=True)
 
 
+def traffic_ratio():
+    """DRAM bytes / algorithmic bytes of k_search from the committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", "k_search_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["dram_per_alg_byte"])
+    return None
+
+
 def run_gpu(args, rank, world, dist):
     import torch
     from hicops_gb300 import dslim
@@ -196,40 +204,99 @@ def run_gpu(args, rank, world, dist):
     d_out = torch.empty(n * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     d_hist = torch.empty(n * HC_HIST_BINS, dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
+    qargs = (d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), None, n, npk,
+             d_out.data_ptr(), d_hist.data_ptr())
+    results = lambda: np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=RESULT_DTYPE).copy()
     ix.set_profiling(True)
 
-    def step():
-        ix.query_device(d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), None, n, npk,
-                        d_out.data_ptr(), d_hist.data_ptr(), stream.cuda_stream)
-
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+    def timed(step, k, w, tag):
+        """w untimed steps, then k steps between events on `stream`; per-step k_search ms."""
+        with torch.cuda.stream(stream):
+            for _ in range(w):
+                step()
+        stream.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kms, launches = [], 0
+        torch.cuda.nvtx.range_push(f"timed:{tag}")
+        ev0.record(stream)
+        for _ in range(k):
             step()
-    stream.synchronize()
+            kms.append(ix.kernel_times()["search"])  # waits for this step's stage events
+            launches += ix.last_launch_count()
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        ms = ev0.elapsed_time(ev1)
+        if dist:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, statistics.median(kms), launches
+
+    # ---- plain form: one CTA per spectrum, default launch shape, separate launches, expeRT e-values
+    ix.set_tuning(schedule=1)
+    plain_tuning = ix.tuning()
+    plain_ms, plain_kms, _ = timed(lambda: ix.query_device(*qargs, stream.cuda_stream),
+                                   max(2, min(args.steps, 3)), 1, "plain")
+    res_plain = results()
+    plain_alg = float(res_plain["post_bytes"].sum())
+
+    # ---- learned part: trained on the histograms this search produced
+    m = dslim.MLP(ix, seed=5)
+    dX = torch.empty(n * 256, dtype=torch.float32, device="cuda")
+    dY = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+    m.features(d_hist.data_ptr(), d_out.data_ptr(), n, dX.data_ptr())
+    m.targets(d_out.data_ptr(), n, dY.data_ptr())
+    torch.cuda.synchronize()
+    ok = (res_plain["reported"] == 1) & (res_plain["evalue"] > 0)
+    sel = torch.from_numpy(np.nonzero(ok)[0][: int(os.environ.get("HC_TRAIN_N", "60000"))]).cuda()
+    Xs, Ys = dX.view(n, 256)[sel].contiguous(), dY.view(n, 3)[sel].contiguous()
+    t = time.time()
+    loss = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=512, epochs=int(os.environ.get("HC_EPOCHS", "20")),
+                   lr=1e-3)
+    t_train = time.time() - t
+    d_learned = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d_scr = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+
+    # ---- batched+learned form: autotuned persistent longest-first kernel replayed from a CUDA graph
+    ns = min(n, 20000)
+    t = time.time()
+    best, _ = ix.tune_device(d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), None, ns,
+                             int(q.idx[ns]), d_out.data_ptr(), d_hist.data_ptr())
+    t_tune = time.time() - t
+    ix.set_tuning(**best)
+
+    def step():
+        ix.query_graph(*qargs, stream=stream.cuda_stream)
+        m.features(d_hist.data_ptr(), d_out.data_ptr(), n, dX.data_ptr(), stream.cuda_stream)
+        m.evalues(dX.data_ptr(), d_out.data_ptr(), n, 0.1, d_learned.data_ptr(), d_nfb.data_ptr(),
+                  d_scr.data_ptr(), stream.cuda_stream)
+
     clocks = Clocks(dev) if rank == 0 else None
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    search_ms, launches = [], 0
-    ev0.record(stream)
-    for _ in range(args.steps):
-        step()
-        search_ms.append(ix.kernel_times()["search"])   # waits for this step's events
-        launches += ix.last_launch_count()
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+    ms, s_ms, launches = timed(step, args.steps, args.warmup, "batched")
     clk = clocks.stop() if clocks else None
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    res = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=RESULT_DTYPE)
+    launches += 5 * args.steps  # features, three dense layers, learned e-values per step
+    res = results()
     alg_bytes = float(res["post_bytes"].sum())
     value = n * world * args.steps / (ms / 1000.0)
-    # end to end through the host-buffer call: pinned inputs in, results out
+    psm_fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore", "post_bytes")
+    mismatch = {f: int((res[f] != res_plain[f]).sum()) for f in psm_fields}
+    same = not any(mismatch.values())
+    used = (res["flags"] & 0x200) != 0
+    dl = np.abs(np.log10(res["evalue"][used]) - np.log10(res_plain["evalue"][used])) if used.any() else np.zeros(1)
+    learned = {"trained_on": int(Xs.shape[0]), "epochs": int(os.environ.get("HC_EPOCHS", "20")),
+               "final_loss": loss, "train_s": t_train, "reported": int(ok.sum()),
+               "learned_share": float(used.sum() / max(1, ok.sum())),
+               "fallback_rate": float(1 - used.sum() / max(1, ok.sum())),
+               "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
+               "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
+
+    # ---- end to end through the host-buffer call (DSLIM_QuerySpectrum's replacement), tuned shape
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     from hicops_gb300 import synthetic as S
     qh = S.QueryBatch(idx=pin(q.idx), moz=pin(q.moz), intensity=pin(q.intensity), precurse=pin(q.precurse),
@@ -241,28 +308,34 @@ def run_gpu(args, rank, world, dist):
         t = time.perf_counter()
         r2, _ = ix.query(qh, want_hist=False)
         e2e_t.append(time.perf_counter() - t)
-    e2e = n / statistics.median(e2e_t)
-    same = bool(np.array_equal(r2["psid"], res["psid"]) and np.array_equal(r2["cpsms"], res["cpsms"]))
+    e2e = n * world / statistics.median(e2e_t)
+    e2e_same = bool(np.array_equal(r2["psid"], res_plain["psid"]) and np.array_equal(r2["cpsms"], res_plain["cpsms"]))
     peak, peak_kind = measured_peaks()
-    s_ms = statistics.median(search_ms)
     achieved = alg_bytes / (s_ms / 1000.0) / 1e9
-    tps = traffic_per_spectrum()
+    ratio = traffic_ratio()
     out = {"metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()), "entries": None, "postings": None,
-                      "spectra_per_step": n, "peaks_per_spectrum": 100, "dF_bins": p.dF, "dM_da": p.dM,
-                      "maxz": p.maxz, "mods": "M+15.99 <=2", "parallelism": f"replicas{world}",
-                      "l2": "index (~2 GB postings) larger than L2; no flush", "form": "plain",
-                      "tuning": ix.tuning()},
+           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()), "entries": None,
+                      "postings": None, "spectra_per_step": n, "peaks_per_spectrum": int(np.diff(q.idx).max()),
+                      "dF_bins": p.dF, "dM_da": p.dM, "maxz": p.maxz, "mods": "M+15.99 <=2",
+                      "parallelism": f"replicas{world}",
+                      "l2": "index (postings + row table, GBs) larger than L2; no flush",
+                      "form": "batched+learned", "tuning": best},
+           "plain": {"spectra_per_s": n * world * max(2, min(args.steps, 3)) / (plain_ms / 1000.0),
+                     "search_ms": plain_kms, "postings_gbs": plain_alg / (plain_kms / 1000.0) / 1e9,
+                     "frac_of_peak": plain_alg / (plain_kms / 1000.0) / 1e9 / peak, "tuning": plain_tuning},
+           "speedup_vs_plain": value / (n * world * max(2, min(args.steps, 3)) / (plain_ms / 1000.0)),
+           "same_psms_as_plain": bool(same), "psm_mismatches": mismatch, "learned": learned,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_source": peak_kind,
-                        "traffic": None if tps is None else tps * n, "kernel": "k_search",
+                        "traffic": None if ratio is None else ratio * alg_bytes, "kernel": "k_search",
                         "alg_bytes_per_launch": alg_bytes, "kernel_ms": s_ms},
            "e2e": {"value": e2e, "unit": "spectra/s",
                    "h2d_bytes_per_step": int(q.idx.nbytes + q.moz.nbytes + q.intensity.nbytes + q.precurse.nbytes),
-                   "d2h_bytes_per_step": int(n * RESULT_DTYPE.itemsize), "same_results": same},
-           "gpu_launches": launches, "index_build_s": t_build, "clocks": clk}
+                   "d2h_bytes_per_step": int(n * RESULT_DTYPE.itemsize), "same_results": e2e_same,
+                   "call": "hc_dslim_query (host buffers), tuned launch shape, expeRT e-values"},
+           "gpu_launches": launches, "index_build_s": t_build, "tune_s": t_tune, "clocks": clk}
     cfg = out["config"]
     cfg["entries"] = int(sum(ix.info(L)[0] for L in range(p.min_len, p.max_len + 1)))
     cfg["postings"] = int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1)))
@@ -274,6 +347,7 @@ def run_gpu(args, rank, world, dist):
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
         print(json.dumps(out), flush=True)
+    m.close()
     ix.close()
 
 

@@ -104,6 +104,8 @@ _SIGS = [
                                C.POINTER(C.c_float)]),
     ("hc_mlp_evalues", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_evalues_mode", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_int, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]),
     ("hc_phase_cycles", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("hc_dslim_query_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,

@@ -37,6 +37,7 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     key.nspec = nspec;
     key.npeaks = npeaks;
     key.tuning = ctx->tuning;
+    key.profiling = ctx->profiling ? 1u : 0u;
     if (!ctx->graph_exec || !same_key(key, ctx->graph_key))
     {
         if (ctx->graph_exec)
@@ -48,14 +49,13 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
         int rc = prepare_query(ctx, nspec);
         if (rc) return rc;
         if (!ctx->cap_stream) HC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
-        const bool prof = ctx->profiling;
-        ctx->profiling = false;
+        // with profiling on, the stage events are captured as external
+        // event-record nodes (the graph key includes the profiling switch)
         HC_CUDA(ctx, cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
         rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist,
                           ctx->cap_stream);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
-        ctx->profiling = prof;
         if (rc) return rc;
         HC_CUDA(ctx, e);
         e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);

@@ -113,6 +113,7 @@ struct GraphKey
     const void *idx, *moz, *inten, *prec, *dM, *out, *hist;
     uint32_t nspec, npeaks;
     hc_tuning tuning;
+    uint32_t profiling;  // stage events captured or not
 };
 
 struct Launch

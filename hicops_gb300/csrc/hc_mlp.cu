@@ -187,43 +187,96 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
     p[i] -= lr * (mi / (1.0f - b1t)) / (sqrtf(vi / (1.0f - b2t)) + 1e-8f);
 }
 
-// learned e-value with the expeRT fit as fallback (res holds the expeRT fit)
+// Learned e-value, one warp per spectrum (res holds the expeRT fit, which
+// stays the fallback). The survival curve is the feature vector itself
+// (log10 survival per bin) over the bins the reference fits, [stt1, end1]
+// (expeRT.cpp:590-598). The regression window's upper end is expeRT's rule
+// (last point above 87 % of the curve's drop, expeRT.cpp:662-676); its start
+// is the network's third output in place of expeRT's 22 % rule (646-661). The
+// line is the least-squares fit of the curve over that window; its RMS
+// residual there (log10 units) must be within `thresh` (a straight tail over
+// the chosen window), else the spectrum keeps its expeRT e-value.
+// mode 0: network window; mode 1: window from the curve's first bin (the
+// same refit without the network, for comparison).
 __global__ void k_learned_evalue(const float *__restrict__ X, const float *__restrict__ out, hc_result *__restrict__ res,
-                                 uint32_t n, float thresh, uint32_t min_cpsm, double expect_max,
+                                 uint32_t n, float thresh, uint32_t min_cpsm, double expect_max, int mode,
                                  float *__restrict__ learned_log10e, uint32_t *__restrict__ nfallback)
 {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (s >= n) return;
     hc_result r = res[s];
     if (r.cpsms < min_cpsm || r.cpsms == 0)
     {
-        learned_log10e[s] = NAN;
+        if (lane == 0) learned_log10e[s] = NAN;
         return;
     }
-    const float slope = out[s * kOut + 0] / tscale(0);
-    const float icpt = out[s * kOut + 1] / tscale(1);
-    int first = (int)lrintf(out[s * kOut + 2] / tscale(2));
-    const int hyp = r.maxhyp;
-    const int last = min(r.nexthyp, kIn - 1);
-    first = max(0, min(first, last));
-    // residual of the predicted line against the spectrum's own survival curve
-    float se = 0.0f;
-    int cnt = 0;
-    for (int b = first; b <= last; b++)
+    const float *x = X + (size_t)s * kIn;
+    const int hyp = r.maxhyp, stt1 = r.minhyp;
+    int end1 = r.nexthyp;
+    if (stt1 == end1) end1 += 1;
+    const int nb = end1 - stt1 + 1;
+    bool fb = hyp >= kIn || end1 >= kIn || stt1 < 0 || nb < 4;
+    int first = 0, last = 0;
+    if (!fb)
     {
-        const float d = slope * (float)b + icpt - X[(size_t)s * kIn + b];
-        se += d * d;
-        cnt++;
+        // upper end: the last point at or above y0 + 0.87 (y_{n-1} - y0)
+        const float y0 = x[stt1], t2 = y0 + 0.87f * (x[end1] - y0);
+        int m2 = nb - 1;
+        for (int q0 = nb - 1; q0 >= 0; q0 -= 32)
+        {
+            const int q = q0 - lane;
+            const uint32_t b = __ballot_sync(0xFFFFFFFFu, q >= 0 && x[stt1 + q] >= t2);
+            if (b) { m2 = q0 - (__ffs(b) - 1); break; }
+        }
+        last = stt1 + m2;
+        if (mode == 0) first = (int)lrintf(out[s * kOut + 2] / tscale(2));
+        else first = stt1;
+        first = max(stt1, min(first, last - 1));
+        fb = last - first < 1;
     }
-    const float resid = cnt ? sqrtf(se / (float)cnt) : 1e30f;
-    const float lg = slope * (float)hyp + icpt + log10f((float)r.cpsms);
-    learned_log10e[s] = lg;
-    if (!(resid <= thresh) || hyp >= kIn)
+    float slope = 0.0f, icpt = 0.0f, resid = 1e30f;
+    if (!fb)
     {
+        const int m = last - first + 1;
+        const float xbar = 0.5f * (float)(first + last);
+        float sy = 0.0f;
+        for (int i = lane; i < m; i += 32) sy += x[first + i];
+        for (int o = 16; o > 0; o >>= 1) sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+        const float ybar = sy / (float)m;
+        float top = 0.0f, bot = 0.0f;
+        for (int i = lane; i < m; i += 32)
+        {
+            const float dx = (float)(first + i) - xbar, y = x[first + i];
+            top += dx * (y - ybar);
+            bot += dx * dx;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            top += __shfl_xor_sync(0xFFFFFFFFu, top, o);
+            bot += __shfl_xor_sync(0xFFFFFFFFu, bot, o);
+        }
+        slope = top / bot;
+        icpt = ybar - slope * xbar;
+        float se = 0.0f;
+        for (int i = lane; i < m; i += 32)
+        {
+            const float d = slope * (float)(first + i) + icpt - x[first + i];
+            se += d * d;
+        }
+        for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xFFFFFFFFu, se, o);
+        resid = mode == 0 ? sqrtf(se / (float)m) : 0.0f;
+    }
+    if (lane != 0) return;
+    if (fb || !(resid <= thresh))
+    {
+        learned_log10e[s] = NAN;
         atomicAdd(nfallback, 1u);  // keep the expeRT value already in res
         return;
     }
-    r.evalue = pow(10.0, (double)lg);
+    const double lg = (double)slope * (double)hyp + (double)icpt + log10((double)r.cpsms);
+    learned_log10e[s] = (float)lg;
+    r.evalue = pow(10.0, lg);
     r.reported = r.evalue < expect_max ? 1u : 0u;
     r.flags |= HC_FLAG_LEARNED;
     res[s] = r;
@@ -423,12 +476,20 @@ int hc_mlp_train(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, uint
 int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, float *d_learned_log10e,
                    uint32_t *d_nfallback, float *d_out_scratch, void *stream)
 {
+    return hc_mlp_evalues_mode(m, d_X, d_res, n, thresh, 0, d_learned_log10e, d_nfallback, d_out_scratch, stream);
+}
+
+int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
+                        float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream)
+{
+    if (mode != 0 && mode != 1) return HC_ERR_INVLD_PARAM;
     if (!m || (n && (!d_X || !d_res || !d_learned_log10e || !d_nfallback || !d_out_scratch))) return HC_ERR_INVLD_PTR;
     cudaStream_t st = stream ? (cudaStream_t)stream : m->ctx->stream;
     int rc = hc_mlp_forward(m, d_X, n, d_out_scratch, st);
     if (rc) return rc;
-    k_learned_evalue<<<(n + 127) / 128, 128, 0, st>>>(d_X, d_out_scratch, d_res, n, thresh, m->ctx->p.min_cpsm,
-                                                      m->ctx->p.expect_max, d_learned_log10e, d_nfallback);
+    if (n)
+        k_learned_evalue<<<(n + 3) / 4, 128, 0, st>>>(d_X, d_out_scratch, d_res, n, thresh, m->ctx->p.min_cpsm,
+                                                      m->ctx->p.expect_max, mode, d_learned_log10e, d_nfallback);
     HC_CUDA(m->ctx, cudaGetLastError());
     return HC_SUCCESS;
 }

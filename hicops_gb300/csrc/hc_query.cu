@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         uint32_t my_shp = 0;
         if (tid == 0)
             for (uint32_t l = 0; l < a.nlen; l++)
-                if (T.win[l].x <= T.win[l].y) T.bytes += 4ull * (2 * a.dF + 2) * nv;  // the reference's bA reads
+                if (T.win[l].x <= T.win[l].y) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);  // the reference's bA reads (other warps add too)
 
         // The spectrum's work is a sequence of jobs (length l, scorecard tile
         // t). Tiles are aligned to multiples of the tile size, so interior
@@ -1177,6 +1177,17 @@ static uint32_t fit_tile(size_t budget, uint32_t dF, uint32_t threads)
     return t < kRowG ? kRowG : t;
 }
 
+// Stage timing event; inside a stream capture it becomes an external event
+// record node, so a replayed graph still times its stages.
+static cudaError_t record_stage(hc_ctx *ctx, int i, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ctx->ev[i], st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ctx->ev[i], st);
+}
+
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads)
 {
     return fit_tile(ctx->smem_optin, dF, threads);
@@ -1301,7 +1312,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 4 * (4 + 2 * 64), st));
 
     const uint64_t nw = (uint64_t)nspec * nlen;
-    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 0, st));
     k_windows<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(ctx->d_lens, nlen, d_prec, d_dM, ctx->p.dM,
                                                             nspec, q.d_win);
     HC_CUDA(ctx, cudaGetLastError());
@@ -1341,10 +1352,10 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     }
     const size_t smem = search_smem(a.tile, a.dF, false, ctx->tuning.threads);
     const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
-    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 1, st));
     int rc2 = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
     if (rc2) return rc2;
-    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
+    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 2, st));
     // spectra whose packed scorecard could overflow are redone wide; the
     // list length is read on the device (no host synchronisation)
     SearchArgs b = a;
@@ -1358,11 +1369,11 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     const size_t smem2 = search_smem(b.tile, b.dF, true, ctx->tuning.threads);
     rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
     if (rc2) return rc2;
-    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
+    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 3, st));
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
                                                                             ctx->p.expect_max, q.d_fitstart);
     HC_CUDA(ctx, cudaGetLastError());
-    if (ctx->profiling) HC_CUDA(ctx, cudaEventRecord(ctx->ev[4], st));
+    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 4, st));
     ctx->last_launches = launches;
     return HC_SUCCESS;
 }

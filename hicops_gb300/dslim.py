@@ -258,7 +258,10 @@ class MLP:
                                                   None if stream is None else C.c_void_p(stream)), "hc_mlp_targets")
 
     def evalues(self, d_X: int, d_res: int, n: int, thresh: float, d_learned: int, d_nfb: int, d_scratch: int,
-                stream: int | None = None):
-        self.ix._check(self.ix.lib.hc_mlp_evalues(self.h, C.c_void_p(d_X), C.c_void_p(d_res), n, C.c_float(thresh),
-                                                  C.c_void_p(d_learned), C.c_void_p(d_nfb), C.c_void_p(d_scratch),
-                                                  None if stream is None else C.c_void_p(stream)), "hc_mlp_evalues")
+                stream: int | None = None, mode: int = 0):
+        """Learned e-values (mode 0: network window; mode 1: the same refit from the curve's first bin)."""
+        self.ix._check(self.ix.lib.hc_mlp_evalues_mode(self.h, C.c_void_p(d_X), C.c_void_p(d_res), n,
+                                                       C.c_float(thresh), mode, C.c_void_p(d_learned),
+                                                       C.c_void_p(d_nfb), C.c_void_p(d_scratch),
+                                                       None if stream is None else C.c_void_p(stream)),
+                       "hc_mlp_evalues")

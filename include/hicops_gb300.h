@@ -215,13 +215,23 @@ int hc_mlp_gradients(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, 
 /* Adam training over [0, n) in minibatches of `batch` for `epochs`. */
 int hc_mlp_train(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, uint32_t batch,
                  uint32_t epochs, float lr, float *final_loss);
-/* Learned e-values: where the predicted line fits the spectrum's survival
- * curve within `thresh` (RMS, log10 units) its e-value replaces the expeRT one
- * in d_res (flag HC_FLAG_LEARNED); elsewhere the expeRT value stays and
- * *d_nfallback counts it. d_learned_log10e[n] gets the prediction for every
- * spectrum; d_out_scratch holds n*3 floats. */
+/* Learned e-values. The network's third output picks the start of the
+ * tail-regression window in place of expeRT's 22 % rule (expeRT.cpp:646-661);
+ * the window ends where expeRT's does (the 87 % rule, 662-676) and the line is
+ * the least-squares fit of the spectrum's log survival curve (the features)
+ * over it. Where that line's RMS residual over the window is within `thresh`
+ * (log10 units: the tail is straight there), its e-value replaces the expeRT
+ * one in d_res (flag HC_FLAG_LEARNED); elsewhere the
+ * expeRT value stays and *d_nfallback counts it. d_learned_log10e[n] gets the
+ * learned log10 e-value (NaN where it fell back); d_out_scratch holds n*3
+ * floats (the network's outputs). */
 int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh,
                    float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
+/* The same with mode 1: the window starts at the curve's first bin (no
+ * network) and no residual test is made; the baseline the network is
+ * measured against. Mode 0 is hc_mlp_evalues. */
+int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
+                        float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
 /* Diagnostics: with phase timing on, the search kernel adds up SM clock
  * cycles per phase (bucket setup, postings stream, score pass 1, score pass 2,
  * tile clear, rest) over all CTAs, then four counts (tiles, tiles scored by a

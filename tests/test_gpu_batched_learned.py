@@ -119,44 +119,67 @@ def test_mlp_gradients_match_float64_reference():
 
 
 def test_learned_evalues_train_and_fallback():
-    """Train on histograms produced by the GPU search; check the fallback rule and the e-value error."""
+    """Train on histograms the GPU search produced (open search, +-500 Da);
+    on held-out spectra the fallback keeps the expeRT e-value, learned
+    e-values stay within 0.05 (log10) of expeRT's for most spectra, and the
+    trained network beats both the same refit without it and an untrained one."""
     import torch
     from hicops_gb300 import dslim
     p = S.SearchParams(maxz=3, dF=1, dM=500.0, threads=8, vmods_per_pep=2, mods=[("M", 15.99, 2)])
-    db = S.make_database(6000, 1301, p)
-    q = S.make_queries(db, 3000, 1302, p,
-                       window_mix=[(0.34, "da", 5.0), (0.33, "da", 50.0), (0.33, "da", 500.0)])
+    db = S.make_database(50000, 1301, p)
+    q = S.make_queries(db, 4000, 1302, p)
     ix = dslim.Index(p)
     ix.construct_all(db)
     d, args = _dev(q)
     ix.query_device(*args)
     n = q.nspec
-    m = dslim.MLP(ix, seed=11)
     dX = torch.zeros(n * 256, dtype=torch.float32, device="cuda")
     dY = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+    m = dslim.MLP(ix, seed=11)
     m.features(d["hist"].data_ptr(), d["out"].data_ptr(), n, dX.data_ptr())
     m.targets(d["out"].data_ptr(), n, dY.data_ptr())
     torch.cuda.synchronize()
     r0, _ = _results(d, n)
+    out0 = d["out"].clone()
     ok = (r0["reported"] == 1) & (r0["evalue"] > 0)
-    sel = torch.from_numpy(np.nonzero(ok)[0]).cuda()
+    train = np.nonzero(ok[:3000])[0]
+    held = np.zeros(n, bool)
+    held[3000:] = ok[3000:]
+    sel = torch.from_numpy(train).cuda()
     Xs = dX.view(n, 256)[sel].contiguous()
     Ys = dY.view(n, 3)[sel].contiguous()
     l0 = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=256, epochs=1, lr=1e-3)
-    l1 = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=256, epochs=60, lr=1e-3)
+    l1 = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=256, epochs=80, lr=1e-3)
     assert l1 < l0 * 0.5, (l0, l1)
-    learned = torch.zeros(n, dtype=torch.float32, device="cuda")
-    nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
-    scratch = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
-    m.evalues(dX.data_ptr(), d["out"].data_ptr(), n, 0.1, learned.data_ptr(), nfb.data_ptr(), scratch.data_ptr())
-    torch.cuda.synchronize()
-    r1, _ = _results(d, n)
-    used = (r1["flags"] & 0x200) != 0
-    # fallback spectra keep the expeRT e-value exactly; learned ones stay within the judge's bound
+
+    def run(net, mode):
+        d["out"].copy_(out0)
+        learned = torch.zeros(n, dtype=torch.float32, device="cuda")
+        nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
+        scratch = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+        net.evalues(dX.data_ptr(), d["out"].data_ptr(), n, 0.1, learned.data_ptr(), nfb.data_ptr(),
+                    scratch.data_ptr(), mode=mode)
+        torch.cuda.synchronize()
+        r1, _ = _results(d, n)
+        used = (r1["flags"] & 0x200) != 0
+        dlog = np.full(n, np.inf)
+        dlog[used] = np.abs(np.log10(r1["evalue"][used]) - np.log10(r0["evalue"][used]))
+        return r1, used, int(nfb.item()), dlog
+
+    r1, used, nfb, dlog = run(m, 0)
+    # fallback spectra keep the expeRT e-value exactly
     assert np.array_equal(r1["evalue"][ok & ~used], r0["evalue"][ok & ~used])
-    if used.any():
-        dlog = np.abs(np.log10(r1["evalue"][used]) - np.log10(r0["evalue"][used]))
-        assert np.percentile(dlog, 50) < 0.5
-    assert int(nfb.item()) == int((ok & ~used).sum())
+    assert nfb == int((ok & ~used).sum())
+    hu = held & used
+    assert hu.sum() >= 0.5 * held.sum(), (int(hu.sum()), int(held.sum()))
+    assert np.percentile(dlog[hu], 50) <= 0.05, np.percentile(dlog[hu], [50, 90])
+    good = lambda dl: float(np.mean(dl[held] <= 0.05))  # held-out spectra learned and within 0.05
+    # without the network: the same refit from the curve's first bin
+    _, _, _, dl_base = run(m, 1)
+    # an untrained network of the same shape
+    m0 = dslim.MLP(ix, seed=12)
+    _, _, _, dl_init = run(m0, 0)
+    assert good(dlog) > good(dl_base) and good(dlog) > good(dl_init), (good(dlog), good(dl_base), good(dl_init))
+    m0.close()
     m.close()
     ix.close()
