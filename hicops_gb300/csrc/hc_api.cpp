@@ -29,7 +29,8 @@ static void free_len(LenHost &lh)
     cudaFree(lh.d_modnum);
     cudaFree(lh.d_seqs);
     cudaFree(lh.d_bA);
-    cudaFree(lh.d_iA);
+    cudaFree(lh.d_qA);
+    cudaFree(lh.d_qp);
     cudaFree(lh.d_rows);
     const uint32_t L = lh.L;
     lh = LenHost();
@@ -281,15 +282,18 @@ int hc_dslim_load(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep, c
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_modnum, 4ull * n + 4));
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_sites, 8ull * n + 8));
     HC_CUDA(ctx, cudaMalloc((void **)&lh->d_bA, 4ull * (nb + 1)));
-    HC_CUDA(ctx, cudaMalloc((void **)&lh->d_iA, 4 * (M + kIaPad)));
     HC_CUDA(ctx, cudaMemcpy(lh->d_mass, m.data(), 4ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_seqid, s.data(), 4ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_modnum, mo.data(), 4ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_sites, si.data(), 8ull * n, cudaMemcpyHostToDevice));
     HC_CUDA(ctx, cudaMemcpy(lh->d_bA, bA, 4ull * (nb + 1), cudaMemcpyHostToDevice));
-    HC_CUDA(ctx, cudaMemcpy(lh->d_iA, iA, 4 * M, cudaMemcpyHostToDevice));
+    uint32_t *d_ids = nullptr;
+    HC_CUDA(ctx, cudaMalloc((void **)&d_ids, 4 * M + 4));
+    HC_CUDA(ctx, cudaMemcpy(d_ids, iA, 4 * M, cudaMemcpyHostToDevice));
     lh->npost = M;
-    if (const int rt = build_row_table(ctx, *lh)) return rt;
+    const int rq = build_query_postings(ctx, *lh, M ? d_ids : nullptr);
+    cudaFree(d_ids);
+    if (rq) return rq;
     lh->built = true;
     ctx->lens_dirty = true;
     return HC_SUCCESS;
@@ -324,7 +328,15 @@ int hc_dslim_export(hc_ctx *ctx, uint32_t L, hc_entry *entries, uint32_t *bA, ui
         for (uint32_t i = 0; i < n; i++) entries[i] = hc_entry{m[i], s[i], si[i], mo[i], 0};
     }
     if (bA) HC_CUDA(ctx, cudaMemcpy(bA, lh->d_bA, 4ull * (nb + 1), cudaMemcpyDeviceToHost));
-    if (iA && lh->npost) HC_CUDA(ctx, cudaMemcpy(iA, lh->d_iA, 4 * lh->npost, cudaMemcpyDeviceToHost));
+    if (iA && lh->npost)
+    {
+        uint32_t *d_ids = nullptr;
+        HC_CUDA(ctx, cudaMalloc((void **)&d_ids, 4 * lh->npost));
+        const int rc = export_ids(ctx, *lh, d_ids);
+        if (rc == HC_SUCCESS) HC_CUDA(ctx, cudaMemcpy(iA, d_ids, 4 * lh->npost, cudaMemcpyDeviceToHost));
+        cudaFree(d_ids);
+        if (rc) return rc;
+    }
     return HC_SUCCESS;
 }
 

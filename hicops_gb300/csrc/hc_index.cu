@@ -346,30 +346,70 @@ __global__ void k_bucket_bounds(const uint32_t *__restrict__ skeys, size_t M, ui
     for (int64_t b = prev + 1; b <= cur; b++) bA[b] = (uint32_t)i;
 }
 
-// Row table: rows[b * stride + k] = first position in bucket b whose entry
-// is >= k * kRowG (ids ascend inside a bucket, so a lower bound on
-// k * kRowG * speclen). Column 0 is bA[b], column stride-1 is bA[b+1].
-__global__ void k_row_table(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ iA, uint32_t nb,
-                            uint32_t stride, uint32_t n, uint32_t speclen, uint32_t *__restrict__ rows)
+// Row table over the query postings: rows[b * stride + k] = first position in
+// bucket b whose entry is >= k * kRowG (a lower bound on k * kRowG << (qsh+1)).
+// Column 0 is qA[b], column stride-1 is qA[b+1] (padding decodes past every
+// entry, so it never precedes a lower bound).
+__global__ void k_row_table(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp, uint32_t nb,
+                            uint32_t stride, uint32_t n, uint32_t qsh, uint32_t *__restrict__ rows)
 {
     const uint64_t total = (uint64_t)nb * stride;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (uint64_t)gridDim.x * blockDim.x)
     {
         const uint32_t b = (uint32_t)(t / stride), k = (uint32_t)(t - (uint64_t)b * stride);
-        uint32_t lo = __ldg(bA + b), hi = __ldg(bA + b + 1);
+        uint32_t lo = __ldg(qA + b), hi = __ldg(qA + b + 1);
         if (k == stride - 1) lo = hi;
         else if (k > 0)
         {
-            const uint32_t v = min(k * kRowG, n) * speclen;  // < 2^31
+            const uint32_t v = min(k * kRowG, n) << (qsh + 1);
             while (lo < hi)
             {
                 const uint32_t m = lo + ((hi - lo) >> 1);
-                if (__ldg(iA + m) < v) lo = m + 1;
+                if (__ldg(qp + m) < v) lo = m + 1;
                 else hi = m;
             }
         }
         rows[t] = lo;
+    }
+}
+
+// padded bucket sizes: ceil4(bA[b+1] - bA[b]); entry nb is 0 (the scan makes it the total)
+__global__ void k_pad_counts(const uint32_t *__restrict__ bA, uint32_t nb, uint32_t *__restrict__ pc)
+{
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += gridDim.x * blockDim.x)
+        pc[b] = b < nb ? ((bA[b + 1] - bA[b] + 3u) & ~3u) : 0u;
+}
+
+// ids (entry*speclen + ion, bucket order) -> query postings, one thread per bucket
+__global__ void k_qpost(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ ids,
+                        const uint32_t *__restrict__ qA, uint32_t nb, uint32_t speclen, uint32_t half,
+                        uint32_t qsh, uint32_t *__restrict__ qp)
+{
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
+    {
+        const uint32_t s = bA[b], e = bA[b + 1], q = qA[b];
+        for (uint32_t i = s; i < e; i++)
+        {
+            const uint32_t id = ids[i], entry = id / speclen, ion = id - entry * speclen;
+            qp[q + (i - s)] = (entry << (qsh + 1)) | ((ion >= half ? 1u : 0u) << qsh) | ion;
+        }
+    }
+}
+
+// query postings -> ids (the reference's iA), one thread per bucket
+__global__ void k_qpost_ids(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ qA,
+                            const uint32_t *__restrict__ qp, uint32_t nb, uint32_t speclen, uint32_t qsh,
+                            uint32_t *__restrict__ ids)
+{
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
+    {
+        const uint32_t s = bA[b], e = bA[b + 1], q = qA[b];
+        for (uint32_t i = s; i < e; i++)
+        {
+            const uint32_t x = qp[q + (i - s)];
+            ids[i] = (x >> (qsh + 1)) * speclen + (x & ((1u << qsh) - 1u));
+        }
     }
 }
 
@@ -410,7 +450,6 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
     HC_CUDA(ctx, dalloc(&lh.d_sites, n));
     HC_CUDA(ctx, dalloc(&lh.d_modnum, n));
     HC_CUDA(ctx, dalloc(&lh.d_bA, (size_t)nb + 1));
-    HC_CUDA(ctx, dalloc(&lh.d_iA, M + kIaPad));  // padded: the query reads 16-byte groups
 
     // scratch: keys/vals ping-pong, radix histograms, scan temp
     const size_t items = M > n ? M : n;
@@ -467,13 +506,19 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         HC_CUDA(ctx, radix_sort(k0, k1, v0, v1, M, bits, hist, stmp, st, &which, &launches, true, true));
         uint32_t *skeys = which ? k1 : k0;
         uint32_t *svals = which ? v1 : v0;
-        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_iA, svals, 4 * M, cudaMemcpyDeviceToDevice, st));
         k_bucket_bounds<<<(unsigned)((M + 1 + 255) / 256), 256, 0, st>>>(skeys, M, nb, lh.d_bA);
-        launches += 2;
+        launches += 1;
+        lh.npost = M;
+        const int rq = build_query_postings(ctx, lh, svals);
+        if (rq) return rq;
+        launches += 4;
     }
     else
     {
         HC_CUDA(ctx, cudaMemsetAsync(lh.d_bA, 0, 4ull * (nb + 1), st));
+        lh.npost = 0;
+        const int rq = build_query_postings(ctx, lh, nullptr);
+        if (rq) return rq;
     }
     uint32_t h_uninit = 0;
     HC_CUDA(ctx, cudaMemcpyAsync(&h_uninit, d_uninit, 4, cudaMemcpyDeviceToHost, st));
@@ -492,26 +537,62 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         cudaFree(d_mod0);
         cudaFree(d_site0);
     }
-    lh.npost = M;
-    int rc = build_row_table(ctx, lh);
-    if (rc) return rc;
     lh.built = true;
     ctx->lens_dirty = true;
     ctx->last_launches = launches + 1;
     return HC_SUCCESS;
 }
 
-int build_row_table(hc_ctx *ctx, LenHost &lh)
+// The query postings (padded buckets), their bucket starts and the row table,
+// from bA (on the device) and the ids in bucket order (d_ids; null when the
+// length has no postings). Leaves d_ids untouched.
+int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
+{
+    cudaStream_t st = ctx->stream;
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
+    uint32_t qsh = 0;
+    while ((1u << qsh) < speclen) qsh++;
+    // 2*entry+isY must stay below the padding's index and x below 2^32
+    if (lh.n + 2ull > (1ull << (31 - qsh)))
+        return set_error(ctx, HC_ERR_INVLD_SIZE, "too many entries of one length for the query postings");
+    lh.qsh = qsh;
+    cudaFree(lh.d_qA);
+    cudaFree(lh.d_qp);
+    cudaFree(lh.d_rows);
+    lh.d_qA = lh.d_qp = lh.d_rows = nullptr;
+    HC_CUDA(ctx, dalloc(&lh.d_qA, (size_t)nb + 1));
+    uint32_t *stmp = nullptr;
+    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words((size_t)nb + 1)));
+    const unsigned bblocks = (unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 16);
+    k_pad_counts<<<bblocks, 256, 0, st>>>(lh.d_bA, nb, lh.d_qA);
+    HC_CUDA(ctx, scan_exclusive(lh.d_qA, (size_t)nb + 1, stmp, st));
+    uint32_t total = 0;
+    HC_CUDA(ctx, cudaMemcpyAsync(&total, lh.d_qA + nb, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    cudaFree(stmp);
+    HC_CUDA(ctx, dalloc(&lh.d_qp, (size_t)total + kIaPad));
+    HC_CUDA(ctx, cudaMemsetAsync(lh.d_qp, 0xFF, 4 * ((size_t)total + kIaPad), st));
+    if (d_ids && lh.npost)
+        k_qpost<<<bblocks, 256, 0, st>>>(lh.d_bA, d_ids, lh.d_qA, nb, speclen, speclen / 2, qsh, lh.d_qp);
+    lh.stride = (lh.n + kRowG - 1) / kRowG + 1;
+    HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
+    const uint64_t rt = (uint64_t)nb * lh.stride;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((rt + 255) / 256, (uint64_t)ctx->sm_count * 64);
+    k_row_table<<<blocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, qsh, lh.d_rows);
+    HC_CUDA(ctx, cudaGetLastError());
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    return HC_SUCCESS;
+}
+
+// The reference's iA (ids entry*speclen + ion, bucket order) from the query postings.
+int export_ids(hc_ctx *ctx, const LenHost &lh, uint32_t *d_ids)
 {
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
     const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
-    cudaFree(lh.d_rows);
-    lh.d_rows = nullptr;
-    lh.stride = (lh.n + kRowG - 1) / kRowG + 1;
-    HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
-    const uint64_t total = (uint64_t)nb * lh.stride;
-    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)ctx->sm_count * 64);
-    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_bA, lh.d_iA, nb, lh.stride, lh.n, speclen, lh.d_rows);
+    const unsigned bblocks = (unsigned)std::min<uint64_t>((nb + 255) / 256, (uint64_t)ctx->sm_count * 16);
+    if (lh.npost)
+        k_qpost_ids<<<bblocks, 256, 0, ctx->stream>>>(lh.d_bA, lh.d_qA, lh.d_qp, nb, speclen, lh.qsh, d_ids);
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HC_SUCCESS;

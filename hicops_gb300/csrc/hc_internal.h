@@ -20,6 +20,13 @@ constexpr size_t kIaPad = 128;     // postings arrays are padded: the query read
 // is >= k * kRowG, for k = 0 .. ceil(n / kRowG). Scorecard tiles are whole
 // multiples of kRowG entries, so every interior tile boundary is a lookup.
 constexpr uint32_t kRowG = 2048;
+// Query postings: the same postings as the reference's iA (ids entry*speclen
+// + ion, ascending inside each bucket), stored as
+//   (entry << (qsh + 1)) | (isY << qsh) | ion     with 2^qsh >= speclen,
+// so that x >> qsh = 2*entry + isY is a candidate's scorecard word index.
+// Every bucket starts at a multiple of 4 words; the gaps hold kQpostPad,
+// which decodes to an index past every tile.
+constexpr uint32_t kQpostPad = 0xFFFFFFFFu;
 
 // One peptide length's device-resident index. All arrays are device pointers.
 struct LenDev
@@ -28,14 +35,16 @@ struct LenDev
     uint32_t npep;
     uint32_t magic, msh;           // floor(x / speclen) = umulhi(x, magic) >> msh, x < 2^31
     uint32_t stride;               // row-table entries per bucket: ceil(n / kRowG) + 1
+    uint32_t qsh;                  // ion bits of the query postings
     const float *mass;
     const uint32_t *seqid;
     const uint64_t *sites;
     const uint32_t *modnum;
     const uint8_t *seqs;
     const uint32_t *bA;
-    const uint32_t *iA;
-    const uint32_t *rows;          // row table, [bucket][k] with `stride` entries per bucket
+    const uint32_t *qA;            // bucket starts in qp (multiples of 4)
+    const uint32_t *qp;            // query postings (see kQpostPad)
+    const uint32_t *rows;          // row table over qp, [bucket][k] with `stride` entries per bucket
 };
 
 // Integer ion-key tables, derived on the host with the reference's double
@@ -72,9 +81,11 @@ struct LenHost
     uint32_t *d_modnum = nullptr;
     uint8_t *d_seqs = nullptr;
     uint32_t *d_bA = nullptr;
-    uint32_t *d_iA = nullptr;
+    uint32_t *d_qA = nullptr;    // padded bucket starts (max_mass*scale + 1)
+    uint32_t *d_qp = nullptr;    // query postings, qA[nb] words (+ kIaPad)
     uint32_t *d_rows = nullptr;  // row table (max_mass*scale buckets x stride)
     uint32_t stride = 0;
+    uint32_t qsh = 0;
     bool built = false;
 };
 
@@ -164,7 +175,8 @@ void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
 
 // hc_index.cu
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
-int build_row_table(hc_ctx *ctx, LenHost &lh);
+int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids);
+int export_ids(hc_ctx *ctx, const LenHost &lh, uint32_t *d_ids);
 
 // hc_query.cu
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads);

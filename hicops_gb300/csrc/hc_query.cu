@@ -37,11 +37,10 @@ namespace hc {
 namespace {
 
 // Per-tile shared-memory lists, sized from the tile (tiles are multiples of 2048):
-//   qualifying candidates tile/8 (u32), past which the tile is scored by a full scan;
 //   chunk -> list map tile/4 (u16), past which a chunk finds its list by search.
-__host__ __device__ constexpr uint32_t qual_cap(uint32_t tile) { return tile / 8; }
 __host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 4; }
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
+constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two)
 constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
 constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
@@ -148,6 +147,8 @@ struct SmemTail
     uint32_t nv;
     uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
     uint32_t ndefer;           // undecided candidates queued for the exact evaluation
+    uint32_t cchunks;          // the job's 16-byte chunks (all lists)
+    uint32_t pad2;
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
@@ -170,7 +171,7 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, cmap, defer, linfo, loff, pmoz, pint, tail, total;
+    size_t qual, cmap, defer, linfo, loff, pmoz, pint, wq, tail, total;
 };
 
 __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide, uint32_t nwarps)
@@ -178,14 +179,14 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
     o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
-    o.cmap = o.qual + 4ull * qual_cap(tile);
+    o.cmap = o.qual;  // (no per-tile candidate list)
     o.defer = o.cmap + 2ull * cmap_cap(tile);
     o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
     o.loff = o.linfo + 16 * maxpairs;
     o.pmoz = o.loff + 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
-    o.tail = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
-    (void)nwarps;
+    o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
+    o.tail = o.wq + 4ull * kWQ * nwarps;
     o.total = o.tail + sizeof(SmemTail);
     return o;
 }
@@ -258,56 +259,13 @@ __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const f
 
 // Position in a bucket of its first posting whose entry is >= c: a row-table
 // entry when c is a multiple of kRowG, else a search inside that row.
-__device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, const uint32_t *__restrict__ iA,
-                                           uint32_t c, uint32_t speclen)
+__device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, const uint32_t *__restrict__ qp,
+                                           uint32_t c, uint32_t qsh)
 {
     const uint32_t k = c / kRowG;
     const uint32_t lo = __ldg(col + k);
     if (c == k * kRowG) return lo;
-    return lower_bound_g(iA, lo, __ldg(col + k + 1), c * speclen);
-}
-
-// In-place exclusive prefix sum of v[0, n) over the block; v[n] = total,
-// which is also returned. Every thread of the block must call it.
-__device__ uint32_t block_exclusive_scan(uint32_t *v, uint32_t n, uint32_t *wsum)
-{
-    const uint32_t tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
-    const uint32_t per = (n + nthr - 1) / nthr;
-    const uint32_t b = min(n, tid * per), e = min(n, b + per);
-    uint32_t sum = 0;
-    for (uint32_t i = b; i < e; i++) sum += v[i];
-    uint32_t x = sum;
-#pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1)
-    {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[wid] = x;
-    __syncthreads();
-    if (wid == 0)
-    {
-        uint32_t y = lane < nw ? wsum[lane] : 0u;
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1)
-        {
-            const uint32_t z = __shfl_up_sync(0xFFFFFFFFu, y, o);
-            if (lane >= o) y += z;
-        }
-        if (lane < nw) wsum[lane] = y;
-    }
-    __syncthreads();
-    uint32_t run = x - sum + (wid ? wsum[wid - 1] : 0u);
-    for (uint32_t i = b; i < e; i++)
-    {
-        const uint32_t t = v[i];
-        v[i] = run;
-        run += t;
-    }
-    const uint32_t total = wsum[nw - 1];
-    if (tid == 0) v[n] = total;
-    __syncthreads();
-    return total;
+    return lower_bound_g(qp, lo, __ldg(col + k + 1), c << (qsh + 1));
 }
 
 // One unit of a spectrum's work: the candidates [c0, c1) of length l, at
@@ -369,18 +327,18 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     const uint32_t nbin = 2 * a.dF + 1;
     const SmemLayout L = smem_layout(tile, a.dF, WIDE, blockDim.x >> 5);
     W *card = reinterpret_cast<W *>(smem);
-    uint32_t *qual = reinterpret_cast<uint32_t *>(smem + L.qual);
+    uint16_t *cmap = reinterpret_cast<uint16_t *>(smem + L.cmap);    // chunk -> list
     uint2 *defer = reinterpret_cast<uint2 *>(smem + L.defer);  // undecided candidates: {b word, y word}
     uint4 *linfo = reinterpret_cast<uint4 *>(smem + L.linfo);  // per list: {first, end, chunk offset, intensity}
     uint32_t *loff = reinterpret_cast<uint32_t *>(smem + L.loff);
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
-    uint16_t *cmap = reinterpret_cast<uint16_t *>(smem + L.cmap);    // chunk -> list
-    const uint32_t qcap = qual_cap(tile), ccap = cmap_cap(tile);
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
+    const uint32_t ccap = cmap_cap(tile);
 
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int lane = tid & 31;
+    const int lane = tid & 31, wid = tid >> 5;
+    uint32_t *wq = reinterpret_cast<uint32_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
     for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
@@ -392,6 +350,74 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         T.pnext = 0;   // reset again after every tile
         T.qcount = 0;
     }
+
+    // Scores one candidate (the float estimate; undecided ones are queued):
+    // cpsms, histogram, flags. A candidate whose estimate comes within kNear
+    // of the running maximum (all candidates of the spectrum so far) gets the
+    // reference's double hyperscore and competes for the top hit. The true top
+    // hit's estimate is within 2*kApproxErr < kNear of the final maximum, so it
+    // is always among them, whatever the order candidates are scored in.
+    uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
+    unsigned long long my_best = 0;
+    uint32_t my_shp = 0;
+    auto score_one = [&](uint32_t bc, uint32_t yc, uint64_t ib, uint64_t iy, uint32_t shp, uint32_t key_lo) {
+        float ha;
+        if constexpr (!WIDE) ha = approx_h(T.lgf, bc, yc, ib, iy);
+        else ha = exact_h(a.qc, bc, yc, ib, iy);
+        const float runmax = __uint_as_float(*(volatile uint32_t *)&T.maxbits);
+        if (ha >= runmax - kNear)
+        {
+            if (ha > runmax) atomicMax(&T.maxbits, __float_as_uint(ha));
+            const float he = WIDE ? ha : exact_h(a.qc, bc, yc, ib, iy);
+            if (he > 0.0f)
+            {
+                const unsigned long long key = ((unsigned long long)__float_as_uint(he) << 32) | key_lo;
+                if (key > my_best)
+                {
+                    my_best = key;
+                    my_shp = shp;
+                }
+                atomicMax(&T.best, key);
+            }
+        }
+        float h;
+        int bin;
+        if constexpr (!WIDE)
+        {
+            const float tt = ha * 10.0f + 0.5f;
+            const float fr = tt - floorf(tt);
+            if (fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin)
+            {
+                const uint32_t di = atomicAdd(&T.ndefer, 1u);
+                if (di < a.defer_cap)
+                {
+                    defer[di] = make_uint2((uint32_t)ib | (bc << 24), (uint32_t)iy | (yc << 24));
+                    return;
+                }
+                my_exact++;  // queue full: exact now
+                h = exact_h(a.qc, bc, yc, ib, iy);
+                bin = hist_bin(h);
+                if (!(h > 0.0f)) return;
+            }
+            else
+            {
+                if (!(ha > 0.0f)) return;
+                h = ha;
+                bin = (int)floorf(tt);
+            }
+        }
+        else
+        {
+            my_exact++;
+            h = ha;
+            bin = hist_bin(h);
+            if (!(h > 0.0f)) return;
+        }
+        my_cps++;
+        if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
+        if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
+        atomicAdd(&T.hist[bin], 1u);
+    };
 
     for (uint32_t iter = 0;; iter++)
     {
@@ -445,11 +471,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         __syncthreads();
         const uint32_t nv = T.nv < HC_QALEN ? T.nv : HC_QALEN;
         const uint32_t np = nv * nbin;
-        unsigned long long my_best = 0;
-        uint32_t my_shp = 0;
+        my_best = 0;
+        my_shp = 0;
         if (tid == 0)
             for (uint32_t l = 0; l < a.nlen; l++)
-                if (T.win[l].x <= T.win[l].y) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);  // the reference's bA reads (other warps add too)
+                if (T.win[l].x <= T.win[l].y) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);  // the reference's bA reads
 
         // The spectrum's work is a sequence of jobs (length l, scorecard tile
         // t). Tiles are aligned to multiples of the tile size, so interior
@@ -466,13 +492,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
-                const uint32_t st = row_lb(col, d.iA, jb.c0, d.speclen);
-                const uint32_t en = row_lb(col, d.iA, jb.c1, d.speclen);
+                const uint32_t st = row_lb(col, d.qp, jb.c0, d.qsh);
+                const uint32_t en = row_lb(col, d.qp, jb.c1, d.qsh);
                 linfo[pr] = make_uint4(st, en, 0u, pint[k]);
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
             }
         }
-        uint32_t C = 0;
+        __syncthreads();
         while (jb.l != kNoJob)
         {
             const LenDev d = a.lens[jb.l];
@@ -480,22 +506,48 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             // ---- chunk offsets of this job's lists ----
             // A list is read in 16-byte chunks (4 postings) from its first
             // posting rounded down to a multiple of 4; the chunks of all
-            // lists are numbered end to end (offsets loff).
+            // lists are numbered end to end (offsets loff). Warp 0 scans the
+            // counts; then every thread maps its lists' chunks.
+            if (wid == 0)
             {
-                uint32_t my_post = 0;
-                for (uint32_t pr = tid; pr < np; pr += nthr) my_post += linfo[pr].y - linfo[pr].x;
-                my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
-                if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);
-                __syncthreads();
-                C = block_exclusive_scan(loff, np, T.wsum);
-                for (uint32_t pr = tid; pr < np; pr += nthr)
+                const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
+                uint32_t sum = 0, post = 0;
+                for (uint32_t i = b; i < e; i++)
                 {
-                    const uint32_t k0 = loff[pr], k1 = min(loff[pr + 1], ccap);
-                    linfo[pr].z = k0;
-                    for (uint32_t k = k0; k < k1; k++) cmap[k] = (uint16_t)pr;
+                    sum += loff[i];
+                    post += linfo[i].y - linfo[i].x;
                 }
-                __syncthreads();
+                uint32_t x = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (lane >= o) x += y;
+                }
+                uint32_t run = x - sum;
+                for (uint32_t i = b; i < e; i++)
+                {
+                    const uint32_t t = loff[i];
+                    loff[i] = run;
+                    run += t;
+                }
+                post = __reduce_add_sync(0xFFFFFFFFu, post);
+                if (lane == 31)
+                {
+                    loff[np] = x;
+                    T.cchunks = x;
+                }
+                if (lane == 0 && post) atomicAdd(&T.bytes, 4ull * post);
             }
+            __syncthreads();
+            const uint32_t C = T.cchunks;
+            for (uint32_t pr = tid; pr < np; pr += nthr)
+            {
+                const uint32_t k0 = loff[pr], k1 = min(loff[pr + 1], ccap);
+                linfo[pr].z = k0;
+                for (uint32_t k = k0; k < k1; k++) cmap[k] = (uint16_t)pr;
+            }
+            __syncthreads();
             HC_PHASE(0);
             // ---- row-table words of the next job's boundaries, in flight ----
             const Job nj = next_job(jb, T.win, a.nlen, tile);
@@ -535,16 +587,14 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 q0 = __shfl_sync(0xFFFFFFFFu, q0, 0);
                 if (q0 >= C) break;
                 uint4 v[G];
-                uint32_t rel[G], span[G], inte[G];  // chunk start - list start, list length, intensity
+                uint32_t inte[G];
 #pragma unroll
                 for (int g = 0; g < G; g++)
                 {
                     const uint32_t kb = q0 + 32u * g;
                     const uint32_t kc = kb + (uint32_t)lane;
-                    rel[g] = 0u;
-                    span[g] = 0u;  // no chunk: every posting fails the range test
                     inte[g] = 0u;
-                    v[g] = make_uint4(0u, 0u, 0u, 0u);
+                    v[g] = make_uint4(kQpostPad, kQpostPad, kQpostPad, kQpostPad);
                     if (kb < C)  // warp-uniform
                     {
                         uint32_t i = 0;
@@ -556,191 +606,125 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                             else
                                 while (i + 1 < np && loff[i + 1] <= kc) i++;
                             const uint4 li = linfo[i];
+                            // a chunk never leaves its bucket (buckets start at
+                            // multiples of 4, padded to them); its postings
+                            // outside [first, end) belong to entries outside
+                            // the tile and fail the index test below
                             const uint32_t pos = (li.x & ~3u) + 4u * (kc - li.z);
-                            rel[g] = pos - li.x;  // wraps below zero for the leading padding
-                            span[g] = li.y - li.x;
                             inte[g] = li.w;
-                            v[g] = __ldg(reinterpret_cast<const uint4 *>(d.iA + pos));
+                            v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
                         }
                     }
                 }
+                const uint32_t base2 = 2 * c0, lim2 = 2 * ntile;
 #pragma unroll
                 for (int g = 0; g < G; g++)
                 {
-                    const uint32_t ids[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
-                    uint32_t loc[4];
-                    W add[4];
-                    bool ok[4];
-#pragma unroll
-                    for (int e = 0; e < 4; e++)
-                    {
-                        const uint32_t ppid = __umulhi(ids[e], d.magic) >> d.msh;
-                        loc[e] = ppid - c0;
-                        ok[e] = (rel[g] + (uint32_t)e) < span[g] && loc[e] < ntile;
-                        const bool isY = (ids[e] - ppid * d.speclen) >= d.half;
-                        loc[e] = 2 * loc[e] + (isY ? 1u : 0u);
-                        if constexpr (!WIDE)
-                            add[e] = (1u << 24) | inte[g];
-                        else
-                            add[e] = (1ull << 40) | (W)inte[g];
-                    }
+                    const uint32_t xs[4] = {v[g].x, v[g].y, v[g].z, v[g].w};
                     if constexpr (!WIDE)
                     {
+                        const uint32_t add = (1u << 24) | inte[g];
 #pragma unroll
                         for (int e = 0; e < 4; e++)
-                            if (ok[e]) ovf |= atomicAdd(&card[loc[e]], add[e]);
+                        {
+                            const uint32_t w = (xs[e] >> d.qsh) - base2;  // 2*(entry - c0) + isY
+                            if (w < lim2) ovf |= atomicAdd(&card[w], add);
+                        }
                     }
                     else
                     {
+                        const W add = (1ull << 40) | (W)inte[g];
 #pragma unroll
                         for (int e = 0; e < 4; e++)
-                            if (ok[e]) atomicAdd(&card[loc[e]], add[e]);
+                        {
+                            const uint32_t w = (xs[e] >> d.qsh) - base2;
+                            if (w < lim2) atomicAdd(&card[w], add);
+                        }
                     }
                 }
             }
             if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
             __syncthreads();
             HC_PHASE(1);
-            // ---- list the candidates that reached min_shp ----
-            // two candidates (four words, 16 bytes) per lane and step; a warp
-            // appends its qualifying candidates with one counter atomic
+            // ---- every candidate that reached min_shp ----
+            // cpsms, histogram and the top hit (see score_one). The packed tile
+            // is scanned two candidates per lane and step; a warp collects its
+            // qualifying candidates in its own ring and scores them 32 at a
+            // time (all lanes busy), then clears the words it scanned.
+            my_cps = my_fl = my_exact = 0;
+            const uint32_t key_l = jb.l << 24;
             if constexpr (!WIDE)
             {
                 const uint4 *c4 = reinterpret_cast<const uint4 *>(card);
-                for (uint32_t base = 2 * (tid - (uint32_t)lane); base < ntile; base += 2 * nthr)
+                uint32_t qh = 0, qhead = 0;  // ring fill and head (warp-uniform)
+                auto pop_score = [&](uint32_t cnt) {
+                    __syncwarp();
+                    if ((uint32_t)lane < cnt)
+                    {
+                        const uint32_t loc = wq[(qhead + lane) & (kWQ - 1)];
+                        uint32_t bc, yc, shp;
+                        uint64_t ib, iy;
+                        decode<false>(card, loc, bc, yc, shp, ib, iy);
+                        score_one(bc, yc, ib, iy, shp, ~(key_l | ((c0 + loc) & 0xFFFFFF)));
+                    }
+                    __syncwarp();
+                };
+                const uint32_t first = 2 * (tid - (uint32_t)lane), step = 2 * nthr;
+                for (uint32_t base = first; base < ntile; base += step)
                 {
                     const uint32_t c = base + 2 * (uint32_t)lane;
                     // words past ntile are zero (the tile is cleared after use)
                     const uint4 w = c < ntile ? c4[c >> 1] : make_uint4(0u, 0u, 0u, 0u);
                     const uint32_t s0 = (w.x >> 24) + (w.y >> 24), s1 = (w.z >> 24) + (w.w >> 24);
-                    const bool q0 = s0 >= a.min_shp && s0 != 0, q1 = s1 >= a.min_shp && s1 != 0;
+                    const bool q0 = s0 >= a.thr, q1 = s1 >= a.thr;  // thr = max(min_shp, 1)
                     const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, q0), b1 = __ballot_sync(0xFFFFFFFFu, q1);
                     if ((b0 | b1) == 0) continue;
                     const uint32_t lt = (1u << lane) - 1u;
-                    uint32_t qb = 0;
-                    if (lane == 0) qb = atomicAdd(&T.qcount, (uint32_t)(__popc(b0) + __popc(b1)));
-                    qb = __shfl_sync(0xFFFFFFFFu, qb, 0);
-                    uint32_t qi = qb + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
-                    if (q0 && qi < qcap) qual[qi] = c;
-                    qi += q0 ? 1u : 0u;
-                    if (q1 && qi < qcap) qual[qi] = c + 1;
+                    const uint32_t r = qhead + qh + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
+                    if (q0) wq[r & (kWQ - 1)] = c;
+                    if (q1) wq[(r + (q0 ? 1u : 0u)) & (kWQ - 1)] = c + 1;
+                    qh += (uint32_t)(__popc(b0) + __popc(b1));
+                    while (qh >= 32)
+                    {
+                        pop_score(32);
+                        qhead += 32;
+                        qh -= 32;
+                    }
                 }
-                __syncthreads();
-            }
-            const uint32_t qn = T.qcount;
-            const bool scan_all = WIDE || qn > qcap;
-            const uint32_t nscore = scan_all ? ntile : qn;
-            if (a.phase && tid == 0)
-            {
-                T.cnt[0] += 1;
-                T.cnt[1] += scan_all ? 1 : 0;
-                T.cnt[2] += qn;
-            }
-            // pass 1: cpsms, histogram and tile maximum from the float
-            // estimate; candidates whose sign or bin the estimate leaves open
-            // are queued (their two words) and resolved exactly once the
-            // spectrum is done
-            {
-                float my_max = 0.0f;
-                uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
-                for (uint32_t i = tid; i < nscore; i += nthr)
+                if (qh) pop_score(qh);
+                // the warp's own words, now read: clear them for the next job
+                uint4 *z4 = reinterpret_cast<uint4 *>(card);
+                for (uint32_t base = first; base < ntile; base += step)
                 {
-                    const uint32_t loc = scan_all ? i : qual[i];
+                    const uint32_t c = base + 2 * (uint32_t)lane;
+                    if (c < ntile) z4[c >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
+            else
+            {
+                // wide words: one candidate per thread, every one checked, then cleared
+                for (uint32_t c = tid; c < ntile; c += nthr)
+                {
                     uint32_t bc, yc, shp;
                     uint64_t ib, iy;
-                    decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
-                    if (shp < a.min_shp || shp == 0) continue;
-                    float h;
-                    int bin;
-                    if constexpr (!WIDE)
-                    {
-                        const float ha = approx_h(T.lgf, bc, yc, ib, iy);
-                        const float tt = ha * 10.0f + 0.5f;
-                        const float fr = tt - floorf(tt);
-                        if (fabsf(ha) <= kApproxErr * 4.0f || fr < kBinMargin || fr > 1.0f - kBinMargin)
-                        {
-                            if (ha > 0.0f) my_max = fmaxf(my_max, ha);
-                            const uint32_t di = atomicAdd(&T.ndefer, 1u);
-                            if (di < a.defer_cap)
-                            {
-                                defer[di] = make_uint2((uint32_t)ib | (bc << 24), (uint32_t)iy | (yc << 24));
-                                continue;
-                            }
-                            my_exact++;  // queue full: exact now
-                            h = exact_h(a.qc, bc, yc, ib, iy);
-                            bin = hist_bin(h);
-                            if (!(h > 0.0f)) continue;
-                        }
-                        else
-                        {
-                            if (!(ha > 0.0f)) continue;
-                            h = ha;
-                            bin = (int)floorf(tt);
-                        }
-                    }
-                    else
-                    {
-                        my_exact++;
-                        h = exact_h(a.qc, bc, yc, ib, iy);
-                        bin = hist_bin(h);
-                        if (!(h > 0.0f)) continue;
-                    }
-                    my_cps++;
-                    if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
-                    if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
-                    atomicAdd(&T.hist[bin], 1u);
-                    my_max = fmaxf(my_max, h);
+                    decode<WIDE>(card, c, bc, yc, shp, ib, iy);
+                    if (shp >= a.min_shp && shp != 0) score_one(bc, yc, ib, iy, shp, ~(key_l | ((c0 + c) & 0xFFFFFF)));
+                    card[2 * c] = 0;
+                    card[2 * c + 1] = 0;
                 }
+            }
+            {
                 my_cps = __reduce_add_sync(0xFFFFFFFFu, my_cps);
                 my_fl = __reduce_or_sync(0xFFFFFFFFu, my_fl);
-                const uint32_t mb = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(my_max));  // my_max >= 0
                 if (lane == 0)
                 {
                     if (my_cps) atomicAdd(&T.cpsms, my_cps);
                     if (my_fl) atomicOr(&T.flags, my_fl);
-                    if (mb) atomicMax(&T.maxbits, mb);
                 }
                 if (a.phase && my_exact) atomicAdd(&T.cnt[3], (unsigned long long)my_exact);
+                if (a.phase && tid == 0) T.cnt[0] += 1;
             }
-            __syncthreads();
             HC_PHASE(2);
-            // pass 2: the reference's double hyperscore for every candidate
-            // that can still be the top hit (within kNear of the maximum so far)
-            {
-                const float runmax = __uint_as_float(T.maxbits);
-                if (runmax > 0.0f)
-                    for (uint32_t i = tid; i < nscore; i += nthr)
-                    {
-                        const uint32_t loc = scan_all ? i : qual[i];
-                        uint32_t bc, yc, shp;
-                        uint64_t ib, iy;
-                        decode<WIDE>(card, loc, bc, yc, shp, ib, iy);
-                        if (shp < a.min_shp || shp == 0) continue;
-                        const float ha = WIDE ? exact_h(a.qc, bc, yc, ib, iy) : approx_h(T.lgf, bc, yc, ib, iy);
-                        if (ha < runmax - kNear) continue;
-                        const float he = WIDE ? ha : exact_h(a.qc, bc, yc, ib, iy);
-                        if (!(he > 0.0f)) continue;
-                        const uint32_t psid = c0 + loc;
-                        const uint32_t tie = (jb.l << 24) | (psid & 0xFFFFFF);
-                        const unsigned long long key =
-                            ((unsigned long long)__float_as_uint(he) << 32) | (unsigned long long)(~tie);
-                        if (key > my_best)
-                        {
-                            my_best = key;
-                            my_shp = shp;
-                        }
-                        atomicMax(&T.best, key);
-                    }
-            }
-            __syncthreads();
-            HC_PHASE(3);
-            if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
-            // ---- clear the tile ----
-            {
-                uint4 *c4 = reinterpret_cast<uint4 *>(card);
-                const uint32_t n4 = (uint32_t)(((size_t)ntile * NW * sizeof(W) + 15) / 16);
-                for (uint32_t i = tid; i < n4; i += nthr) c4[i] = make_uint4(0, 0, 0, 0);
-            }
             if (tid == 0)
             {
                 T.qcount = 0;
@@ -748,7 +732,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
             // ---- the next job's list bounds from the prefetched words ----
             // (each thread rewrites only its own lists; the stream that read
-            // linfo/loff ended at the barrier above)
+            // linfo/loff ended at a barrier above)
             if (nj.l != kNoJob)
             {
 #pragma unroll
@@ -760,10 +744,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         const uint32_t st = same ? linfo[pr].y
                                                  : (nj.c0 % kRowG == 0u
                                                         ? ps_lo[m]
-                                                        : lower_bound_g(dn.iA, ps_lo[m], ps_hi[m], nj.c0 * dn.speclen));
+                                                        : lower_bound_g(dn.qp, ps_lo[m], ps_hi[m], nj.c0 << (dn.qsh + 1)));
                         const uint32_t en = (nj.c1 % kRowG == 0u)
                                                 ? pf_lo[m]
-                                                : lower_bound_g(dn.iA, pf_lo[m], pf_hi[m], nj.c1 * dn.speclen);
+                                                : lower_bound_g(dn.qp, pf_lo[m], pf_hi[m], nj.c1 << (dn.qsh + 1));
                         linfo[pr] = make_uint4(st, en, 0u, pint[pr / nbin]);
                         loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                     }
@@ -773,45 +757,47 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 {
                     const uint32_t k = pr / nbin, j = pr - k * nbin;
                     const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                    const uint32_t st = same ? linfo[pr].y : row_lb(col, dn.iA, nj.c0, dn.speclen);
-                    const uint32_t en = row_lb(col, dn.iA, nj.c1, dn.speclen);
+                    const uint32_t st = same ? linfo[pr].y : row_lb(col, dn.qp, nj.c0, dn.qsh);
+                    const uint32_t en = row_lb(col, dn.qp, nj.c1, dn.qsh);
                     linfo[pr] = make_uint4(st, en, 0u, pint[k]);
                     loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                 }
             }
             __syncthreads();
-            HC_PHASE(4);
+            HC_PHASE(3);
             jb = nj;
         }
         // ---- candidates whose sign or bin the float estimate left open ----
         if (!WIDE)
         {
             const uint32_t nd = min(T.ndefer, a.defer_cap);
-            uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
+            uint32_t cps = 0, fl = 0, nex = 0;
             for (uint32_t i = tid; i < nd; i += nthr)
             {
                 uint32_t bc, yc, shp;
                 uint64_t ib, iy;
                 const uint2 w = defer[i];
                 decode_packed(w.x, w.y, bc, yc, shp, ib, iy);
-                my_exact++;
+                nex++;
                 const float h = exact_h(a.qc, bc, yc, ib, iy);
                 if (!(h > 0.0f)) continue;
                 int bin = hist_bin(h);
-                my_cps++;
-                if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
-                if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
+                cps++;
+                if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) fl |= HC_FLAG_LGFACT_OOB;
+                if (bin >= HC_HIST_BINS || bin < 0) { fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
                 atomicAdd(&T.hist[bin], 1u);
             }
-            my_cps = __reduce_add_sync(0xFFFFFFFFu, my_cps);
-            my_fl = __reduce_or_sync(0xFFFFFFFFu, my_fl);
+            cps = __reduce_add_sync(0xFFFFFFFFu, cps);
+            fl = __reduce_or_sync(0xFFFFFFFFu, fl);
             if (lane == 0)
             {
-                if (my_cps) atomicAdd(&T.cpsms, my_cps);
-                if (my_fl) atomicOr(&T.flags, my_fl);
+                if (cps) atomicAdd(&T.cpsms, cps);
+                if (fl) atomicOr(&T.flags, fl);
             }
-            if (a.phase && my_exact) atomicAdd(&T.cnt[3], (unsigned long long)my_exact);
+            if (a.phase && nex) atomicAdd(&T.cnt[3], (unsigned long long)nex);
         }
+        // the top hit's shared ions come from the thread that found it
+        if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
         __syncthreads();
         HC_PHASE(5);
         // ---- write the spectrum's results ----
@@ -1260,7 +1246,9 @@ static void fill_lendev(const hc_ctx *ctx, const LenHost &lh, LenDev &d)
     d.modnum = lh.d_modnum;
     d.seqs = lh.d_seqs;
     d.bA = lh.d_bA;
-    d.iA = lh.d_iA;
+    d.qA = lh.d_qA;
+    d.qp = lh.d_qp;
+    d.qsh = lh.qsh;
     d.rows = lh.d_rows;
 }
 
