@@ -181,6 +181,77 @@ def traffic_ratio():
     return None
 
 
+def subset(q, mask):
+    """The spectra of a CSR batch where mask is true (same order)."""
+    from hicops_gb300 import synthetic as S
+    sel = np.nonzero(mask)[0]
+    lo, hi = q.idx[sel].astype(np.int64), q.idx[sel + 1].astype(np.int64)
+    cnt = hi - lo
+    idx = np.zeros(sel.size + 1, np.uint32)
+    idx[1:] = np.cumsum(cnt)
+    take = np.concatenate([np.arange(a, b) for a, b in zip(lo, hi)]) if sel.size else np.zeros(0, np.int64)
+    return S.QueryBatch(idx=idx, moz=q.moz[take], intensity=q.intensity[take], precurse=q.precurse[sel],
+                        charges=q.charges[sel], rtimes=q.rtimes[sel], dM=q.dM[sel])
+
+
+def run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning):
+    """Config 2: the open-2m index, 200,000 spectra with 20-150 peaks and mixed windows
+    (50 % +-10 ppm, 30 % +-50 Da, 20 % +-500 Da). Plain: one launch per window class
+    (one CTA per spectrum, default shape); batched: one persistent longest-first launch
+    with the autotuned shape, replayed from a CUDA graph."""
+    import torch
+    from hicops_gb300 import synthetic as S
+    from hicops_gb300._lib import RESULT_DTYPE, HC_HIST_BINS
+    nm = int(os.environ.get("HC_MIXED_N", "200000"))
+    qm = S.make_queries(db, nm, 0xC21 + 1000 * rank, p, peaks=(20, 150),
+                        window_mix=[(0.5, "ppm", 10.0), (0.3, "da", 50.0), (0.2, "da", 500.0)])
+    cls = np.where(qm.dM < 1.0, 0, np.where(qm.dM < 100.0, 1, 2))
+
+    def dev(q):
+        n = q.nspec
+        d = dict(idx=torch.from_numpy(q.idx.astype(np.int32)).cuda(),
+                 moz=torch.from_numpy(q.moz.view(np.int32)).cuda(),
+                 inten=torch.from_numpy(q.intensity.view(np.int32)).cuda(),
+                 prec=torch.from_numpy(q.precurse).cuda(), dM=torch.from_numpy(q.dM).cuda(),
+                 out=torch.empty(max(1, n) * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda"),
+                 hist=torch.empty(max(1, n) * HC_HIST_BINS, dtype=torch.int32, device="cuda"))
+        a = (d["idx"].data_ptr(), d["moz"].data_ptr(), d["inten"].data_ptr(), d["prec"].data_ptr(),
+             d["dM"].data_ptr(), n, int(q.moz.shape[0]), d["out"].data_ptr(), d["hist"].data_ptr())
+        return d, a
+
+    parts = [subset(qm, cls == c) for c in range(3)]
+    dparts = [dev(x) for x in parts]
+    dfull, afull = dev(qm)
+    res_of = lambda d, n: np.frombuffer(d["out"].cpu().numpy().tobytes(), dtype=RESULT_DTYPE)[:n].copy()
+    steps = max(2, min(args.steps, 3))
+    saved = ix.tuning()
+    ix.set_tuning(**plain_tuning)  # schedule 1, default shape
+
+    def plain_step():
+        for (d, a) in dparts:
+            ix.query_device(*a, stream.cuda_stream)
+
+    p_ms, _, _ = timed(plain_step, steps, 1, "mixed_plain")
+    plain_res = [res_of(d, x.nspec) for (d, _), x in zip(dparts, parts)]
+    ns = min(nm, 40000)
+    best, _ = ix.tune_device(afull[0], afull[1], afull[2], afull[3], afull[4], ns, int(qm.idx[ns]),
+                             afull[7], afull[8])
+    ix.set_tuning(**best)
+    b_ms, _, _ = timed(lambda: ix.query_graph(*afull, stream=stream.cuda_stream), steps, 1, "mixed_batched")
+    res = res_of(dfull, nm)
+    fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore")
+    mism = 0
+    for c in range(3):
+        r = res[cls == c]
+        mism += int(sum((r[f] != plain_res[c][f]).sum() for f in fields))
+    ix.set_tuning(**saved)
+    pv, bv = nm * world * steps / (p_ms / 1000.0), nm * world * steps / (b_ms / 1000.0)
+    return {"spectra": nm, "classes": {"ppm10": int((cls == 0).sum()), "da50": int((cls == 1).sum()),
+                                       "da500": int((cls == 2).sum())},
+            "plain_per_class_spectra_per_s": pv, "batched_spectra_per_s": bv, "speedup": bv / pv,
+            "same_psms": mism == 0, "psm_field_mismatches": mism, "batched_tuning": best}
+
+
 def run_gpu(args, rank, world, dist):
     import torch
     from hicops_gb300 import dslim
@@ -296,6 +367,12 @@ def run_gpu(args, rank, world, dist):
                "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
                "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
 
+    # ---- uneven batch (mixed precursor windows, 20-150 peaks) on the same index:
+    # one plain launch per window class against one batched launch
+    mixed = None
+    if os.environ.get("HC_MIXED", "1") == "1":
+        mixed = run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning)
+
     # ---- end to end through the host-buffer call (DSLIM_QuerySpectrum's replacement), tuned shape
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     from hicops_gb300 import synthetic as S
@@ -327,6 +404,7 @@ def run_gpu(args, rank, world, dist):
                      "frac_of_peak": plain_alg / (plain_kms / 1000.0) / 1e9 / peak, "tuning": plain_tuning},
            "speedup_vs_plain": value / (n * world * max(2, min(args.steps, 3)) / (plain_ms / 1000.0)),
            "same_psms_as_plain": bool(same), "psm_mismatches": mismatch, "learned": learned,
+           "mixed_windows": mixed,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_source": peak_kind,
                         "traffic": None if ratio is None else ratio * alg_bytes, "kernel": "k_search",

@@ -101,6 +101,8 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     ctx->p = *p;
     ctx->sm_count = prop.multiProcessorCount;
     ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    ctx->smem_sm = prop.sharedMemPerMultiprocessor;
+    ctx->smem_reserved = prop.reservedSharedMemPerBlock;
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return HC_ERR_NO_DEVICE; }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
     {
@@ -132,12 +134,12 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     const uint32_t nlen = p->max_len - p->min_len + 1;
     ctx->lens.resize(nlen);
     for (uint32_t i = 0; i < nlen; i++) ctx->lens[i].L = p->min_len + i;
-    // default launch shape: one 512-thread CTA per SM, 4 postings lists in
-    // flight per warp, the largest scorecard tile the shared memory holds
-    ctx->tuning.threads = 512;
-    ctx->tuning.tile = max_tile(ctx, p->dF, 512);
+    // default launch shape: one 1024-thread CTA per SM, 2 postings chunks in
+    // flight per lane, the largest scorecard tile the shared memory holds
+    ctx->tuning.threads = 1024;
+    ctx->tuning.tile = max_tile(ctx, p->dF, 1024);
     ctx->tuning.ctas_per_sm = 1;
-    ctx->tuning.pairs_per_warp = 4;
+    ctx->tuning.pairs_per_warp = 2;
     ctx->tuning.schedule = 0;
     ctx->tuning.defer_cap = HC_DEFER_MAX;
     *out = ctx;
@@ -181,7 +183,7 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
         t->schedule > 2 || t->defer_cap > HC_DEFER_MAX)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "bad tuning");
     const size_t need = search_smem(t->tile, ctx->p.dF, false, t->threads);
-    if (need * t->ctas_per_sm > ctx->smem_optin + 1024 * (t->ctas_per_sm - 1) || need > ctx->smem_optin)
+    if (t->ctas_per_sm * (need + ctx->smem_reserved) > ctx->smem_sm || need > ctx->smem_optin)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "tile does not fit in shared memory");
     ctx->tuning = *t;
     return HC_SUCCESS;

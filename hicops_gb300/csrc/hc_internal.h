@@ -140,7 +140,9 @@ struct hc_ctx
 {
     int device = 0;
     int sm_count = 0;
-    size_t smem_optin = 0;
+    size_t smem_optin = 0;     // per CTA, opt-in maximum
+    size_t smem_sm = 0;        // per SM
+    size_t smem_reserved = 0;  // per CTA, kept by the system
     hc_params p{};
     cudaStream_t stream = nullptr;
     hc_tuning tuning{};

@@ -147,8 +147,7 @@ struct SmemTail
     uint32_t nv;
     uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
     uint32_t ndefer;           // undecided candidates queued for the exact evaluation
-    uint32_t cchunks;          // the job's 16-byte chunks (all lists)
-    uint32_t pad2;
+    uint32_t cchunks[2];       // 16-byte chunks (all lists) of the job in each bound buffer
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
@@ -172,6 +171,7 @@ struct SmemTail
 struct SmemLayout
 {
     size_t qual, cmap, defer, linfo, loff, pmoz, pint, wq, tail, total;
+    uint32_t maxpairs, loffs;  // linfo / loff entries per buffer (two buffers each)
 };
 
 __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide, uint32_t nwarps)
@@ -181,9 +181,11 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
     o.cmap = o.qual;  // (no per-tile candidate list)
     o.defer = o.cmap + 2ull * cmap_cap(tile);
+    o.maxpairs = (uint32_t)maxpairs;
+    o.loffs = (uint32_t)maxpairs + 4;
     o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
-    o.loff = o.linfo + 16 * maxpairs;
-    o.pmoz = o.loff + 4 * (maxpairs + 4);
+    o.loff = o.linfo + 2 * 16 * maxpairs;
+    o.pmoz = o.loff + 2 * 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
     o.tail = o.wq + 4ull * kWQ * nwarps;
@@ -266,6 +268,54 @@ __device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, con
     const uint32_t lo = __ldg(col + k);
     if (c == k * kRowG) return lo;
     return lower_bound_g(qp, lo, __ldg(col + k + 1), c << (qsh + 1));
+}
+
+// Warp-level: exclusive chunk offsets of lists [0, np) in place (lo[np] =
+// total), linfo[i].z = offset; the total goes to *total and the postings
+// visited (4 bytes each) to *bytes. Must be called by all 32 lanes of a warp.
+__device__ void chunk_offsets(uint4 *linfo, uint32_t *lo, uint32_t np, int lane, uint32_t *total,
+                              unsigned long long *bytes)
+{
+    const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
+    uint32_t sum = 0, post = 0;
+    for (uint32_t i = b; i < e; i++)
+    {
+        sum += lo[i];
+        post += linfo[i].y - linfo[i].x;
+    }
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    uint32_t run = x - sum;
+    for (uint32_t i = b; i < e; i++)
+    {
+        const uint32_t t = lo[i];
+        lo[i] = run;
+        linfo[i].z = run;
+        run += t;
+    }
+    post = __reduce_add_sync(0xFFFFFFFFu, post);
+    if (lane == 31)
+    {
+        lo[np] = x;
+        *total = x;
+    }
+    if (lane == 0 && post) atomicAdd(bytes, 4ull * post);
+}
+
+// Asks L2 for the 128-byte lines holding postings [st, en) of qp (the 16-byte
+// chunks the stream will read: from st rounded down to a multiple of 4).
+__device__ __forceinline__ void prefetch_l2(const uint32_t *qp, uint32_t st, uint32_t en)
+{
+    if (st >= en) return;
+    const char *p0 = reinterpret_cast<const char *>(qp + (st & ~3u));
+    const char *p1 = reinterpret_cast<const char *>(qp + en);
+    for (const char *p = reinterpret_cast<const char *>((uintptr_t)p0 & ~(uintptr_t)127); p < p1; p += 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
 // One unit of a spectrum's work: the candidates [c0, c1) of length l, at
@@ -480,10 +530,14 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // The spectrum's work is a sequence of jobs (length l, scorecard tile
         // t). Tiles are aligned to multiples of the tile size, so interior
         // tile boundaries are row-table entries; only a window's own ends need
-        // a search inside one row. While job j streams, every thread already
-        // has the row-table words of job j+1's boundaries in flight.
+        // a search inside one row. The per-list bounds are double-buffered:
+        // while job j streams, the row-table words of job j+1's boundaries are
+        // in flight; right after the stream each thread turns them into job
+        // j+1's bounds and asks L2 for those postings, which then arrive while
+        // the block scores job j.
         Job jb = first_job(T.win, a.nlen, tile);
         uint32_t pf_lo[kPf], pf_hi[kPf], ps_lo[kPf], ps_hi[kPf];
+        uint32_t cur = 0;
         if (jb.l != kNoJob)
         {
             // the first job's boundaries, directly
@@ -497,55 +551,37 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 linfo[pr] = make_uint4(st, en, 0u, pint[k]);
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
             }
+            __syncthreads();
+            if (wid == 0) chunk_offsets(linfo, loff, np, lane, &T.cchunks[0], &T.bytes);
         }
         __syncthreads();
         while (jb.l != kNoJob)
         {
             const LenDev d = a.lens[jb.l];
             const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
-            // ---- chunk offsets of this job's lists ----
-            // A list is read in 16-byte chunks (4 postings) from its first
-            // posting rounded down to a multiple of 4; the chunks of all
-            // lists are numbered end to end (offsets loff). Warp 0 scans the
-            // counts; then every thread maps its lists' chunks.
-            if (wid == 0)
+            uint4 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
+            uint32_t *lo_c = loff + cur * L.loffs, *lo_n = loff + (cur ^ 1) * L.loffs;
+            const uint32_t C = T.cchunks[cur];
+            // ---- chunk -> list map: each thread a contiguous run of chunks ----
             {
-                const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
-                uint32_t sum = 0, post = 0;
-                for (uint32_t i = b; i < e; i++)
+                const uint32_t cm = min(C, ccap), per = (cm + nthr - 1) / nthr;
+                const uint32_t k0 = min(cm, (uint32_t)tid * per), k1 = min(cm, k0 + per);
+                if (k0 < k1)
                 {
-                    sum += loff[i];
-                    post += linfo[i].y - linfo[i].x;
+                    uint32_t lo = 0, hi = np;  // last list with lo_c[i] <= k0
+                    while (hi - lo > 1)
+                    {
+                        const uint32_t m = (lo + hi) >> 1;
+                        if (lo_c[m] <= k0) lo = m;
+                        else hi = m;
+                    }
+                    uint32_t i = lo;
+                    for (uint32_t k = k0; k < k1; k++)
+                    {
+                        while (lo_c[i + 1] <= k) i++;
+                        cmap[k] = (uint16_t)i;
+                    }
                 }
-                uint32_t x = sum;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1)
-                {
-                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                    if (lane >= o) x += y;
-                }
-                uint32_t run = x - sum;
-                for (uint32_t i = b; i < e; i++)
-                {
-                    const uint32_t t = loff[i];
-                    loff[i] = run;
-                    run += t;
-                }
-                post = __reduce_add_sync(0xFFFFFFFFu, post);
-                if (lane == 31)
-                {
-                    loff[np] = x;
-                    T.cchunks = x;
-                }
-                if (lane == 0 && post) atomicAdd(&T.bytes, 4ull * post);
-            }
-            __syncthreads();
-            const uint32_t C = T.cchunks;
-            for (uint32_t pr = tid; pr < np; pr += nthr)
-            {
-                const uint32_t k0 = loff[pr], k1 = min(loff[pr + 1], ccap);
-                linfo[pr].z = k0;
-                for (uint32_t k = k0; k < k1; k++) cmap[k] = (uint16_t)pr;
             }
             __syncthreads();
             HC_PHASE(0);
@@ -599,13 +635,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         uint32_t i = 0;
                         if (kb + 32u > ccap)  // past the map: search
-                            i = find_list(loff, np, kb, lane);
+                            i = find_list(lo_c, np, kb, lane);
                         if (kc < C)
                         {
                             if (kc < ccap) i = cmap[kc];
                             else
-                                while (i + 1 < np && loff[i + 1] <= kc) i++;
-                            const uint4 li = linfo[i];
+                                while (i + 1 < np && lo_c[i + 1] <= kc) i++;
+                            const uint4 li = li_c[i];
                             // a chunk never leaves its bucket (buckets start at
                             // multiples of 4, padded to them); its postings
                             // outside [first, end) belong to entries outside
@@ -644,8 +680,43 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 }
             }
             if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
+            // ---- the next job's list bounds, and its postings into L2 ----
+            if (nj.l != kNoJob)
+            {
+#pragma unroll
+                for (int m = 0; m < kPf; m++)
+                {
+                    const uint32_t pr = tid + m * nthr;
+                    if (pr < np)
+                    {
+                        const uint32_t st = same ? li_c[pr].y
+                                                 : (nj.c0 % kRowG == 0u
+                                                        ? ps_lo[m]
+                                                        : lower_bound_g(dn.qp, ps_lo[m], ps_hi[m], nj.c0 << (dn.qsh + 1)));
+                        const uint32_t en = (nj.c1 % kRowG == 0u)
+                                                ? pf_lo[m]
+                                                : lower_bound_g(dn.qp, pf_lo[m], pf_hi[m], nj.c1 << (dn.qsh + 1));
+                        li_n[pr] = make_uint4(st, en, 0u, pint[pr / nbin]);
+                        lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                        prefetch_l2(dn.qp, st, en);
+                    }
+                }
+                // lists past kPf * nthr (small blocks, wide bin windows): directly
+                for (uint32_t pr = tid + kPf * nthr; pr < np; pr += nthr)
+                {
+                    const uint32_t k = pr / nbin, j = pr - k * nbin;
+                    const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
+                    const uint32_t st = same ? li_c[pr].y : row_lb(col, dn.qp, nj.c0, dn.qsh);
+                    const uint32_t en = row_lb(col, dn.qp, nj.c1, dn.qsh);
+                    li_n[pr] = make_uint4(st, en, 0u, pint[k]);
+                    lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                    prefetch_l2(dn.qp, st, en);
+                }
+            }
             __syncthreads();
             HC_PHASE(1);
+            // ---- the next job's chunk offsets (warp 0, before its scoring share) ----
+            if (wid == 0 && nj.l != kNoJob) chunk_offsets(li_n, lo_n, np, lane, &T.cchunks[cur ^ 1], &T.bytes);
             // ---- every candidate that reached min_shp ----
             // cpsms, histogram and the top hit (see score_one). The packed tile
             // is scanned two candidates per lane and step; a warp collects its
@@ -725,46 +796,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 if (a.phase && tid == 0) T.cnt[0] += 1;
             }
             HC_PHASE(2);
-            if (tid == 0)
-            {
-                T.qcount = 0;
-                T.pnext = 0;
-            }
-            // ---- the next job's list bounds from the prefetched words ----
-            // (each thread rewrites only its own lists; the stream that read
-            // linfo/loff ended at a barrier above)
-            if (nj.l != kNoJob)
-            {
-#pragma unroll
-                for (int m = 0; m < kPf; m++)
-                {
-                    const uint32_t pr = tid + m * nthr;
-                    if (pr < np)
-                    {
-                        const uint32_t st = same ? linfo[pr].y
-                                                 : (nj.c0 % kRowG == 0u
-                                                        ? ps_lo[m]
-                                                        : lower_bound_g(dn.qp, ps_lo[m], ps_hi[m], nj.c0 << (dn.qsh + 1)));
-                        const uint32_t en = (nj.c1 % kRowG == 0u)
-                                                ? pf_lo[m]
-                                                : lower_bound_g(dn.qp, pf_lo[m], pf_hi[m], nj.c1 << (dn.qsh + 1));
-                        linfo[pr] = make_uint4(st, en, 0u, pint[pr / nbin]);
-                        loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                    }
-                }
-                // lists past kPf * nthr (small blocks, wide bin windows): directly
-                for (uint32_t pr = tid + kPf * nthr; pr < np; pr += nthr)
-                {
-                    const uint32_t k = pr / nbin, j = pr - k * nbin;
-                    const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                    const uint32_t st = same ? linfo[pr].y : row_lb(col, dn.qp, nj.c0, dn.qsh);
-                    const uint32_t en = row_lb(col, dn.qp, nj.c1, dn.qsh);
-                    linfo[pr] = make_uint4(st, en, 0u, pint[k]);
-                    loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                }
-            }
+            if (tid == 0) T.pnext = 0;
             __syncthreads();
             HC_PHASE(3);
+            cur ^= 1;
             jb = nj;
         }
         // ---- candidates whose sign or bin the float estimate left open ----
@@ -1182,8 +1217,8 @@ uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads)
 uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm, uint32_t threads)
 {
     if (ctas_per_sm <= 1) return max_tile(ctx, dF, threads);
-    // the SM's shared memory (optin + 1 KB) is split; each CTA keeps 1 KB for the system
-    const size_t per = (ctx->smem_optin + 1024) / ctas_per_sm - 1024;
+    // the SM's shared memory is split; each CTA also keeps a reserve for the system
+    const size_t per = std::min(ctx->smem_optin, ctx->smem_sm / ctas_per_sm - ctx->smem_reserved);
     const uint32_t t = fit_tile(per, dF, threads);
     return smem_layout(t, dF, false, threads / 32).total <= per ? t : 0u;
 }
