@@ -178,6 +178,7 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
 {
     if (!ctx || !t) return HC_ERR_INVLD_PTR;
     if (t->threads < 64 || t->threads > 1024 || (t->threads & 31) || t->tile < kRowG || (t->tile % kRowG) ||
+        t->tile > 32768 ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
         (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8) ||
         t->schedule > 2 || t->defer_cap > HC_DEFER_MAX)

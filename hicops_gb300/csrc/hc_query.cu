@@ -37,8 +37,8 @@ namespace hc {
 namespace {
 
 // Per-tile shared-memory lists, sized from the tile (tiles are multiples of 2048):
-//   chunk -> list map tile/4 (u16), past which a chunk finds its list by search.
-__host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 4; }
+//   chunk -> list map tile/2 (u16), past which a chunk finds its list by search.
+__host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 2; }
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
 constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two)
 constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
@@ -188,7 +188,7 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     o.pmoz = o.loff + 2 * 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
-    o.tail = o.wq + 4ull * kWQ * nwarps;
+    o.tail = (o.wq + 2ull * kWQ * nwarps + 15) & ~(size_t)15;
     o.total = o.tail + sizeof(SmemTail);
     return o;
 }
@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5;
-    uint32_t *wq = reinterpret_cast<uint32_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring
+    uint16_t *wq = reinterpret_cast<uint16_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring (tile < 2^16)
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
     for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
@@ -752,8 +752,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     if ((b0 | b1) == 0) continue;
                     const uint32_t lt = (1u << lane) - 1u;
                     const uint32_t r = qhead + qh + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
-                    if (q0) wq[r & (kWQ - 1)] = c;
-                    if (q1) wq[(r + (q0 ? 1u : 0u)) & (kWQ - 1)] = c + 1;
+                    if (q0) wq[r & (kWQ - 1)] = (uint16_t)c;
+                    if (q1) wq[(r + (q0 ? 1u : 0u)) & (kWQ - 1)] = (uint16_t)(c + 1);
                     qh += (uint32_t)(__popc(b0) + __popc(b1));
                     while (qh >= 32)
                     {
@@ -1193,7 +1193,7 @@ static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need);
 // the largest tile (a multiple of kRowG) whose whole layout fits in `budget` bytes
 static uint32_t fit_tile(size_t budget, uint32_t dF, uint32_t threads)
 {
-    uint32_t t = (uint32_t)std::min<size_t>(budget / 8, 1u << 24) / kRowG * kRowG;
+    uint32_t t = (uint32_t)std::min<size_t>(budget / 8, 32768) / kRowG * kRowG;  // ring entries are 16-bit
     while (t > kRowG && smem_layout(t, dF, false, threads / 32).total > budget) t -= kRowG;
     return t < kRowG ? kRowG : t;
 }
