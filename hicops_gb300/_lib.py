@@ -84,6 +84,9 @@ _SIGS = [
                                     C.c_int64]),
     ("hc_dslim_query", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_dslim_query_stream", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
     ("hc_dslim_query_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),

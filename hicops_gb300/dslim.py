@@ -118,6 +118,24 @@ class Index:
                                             L.ptr(dM), n, L.ptr(out), L.ptr(hist)), "hc_dslim_query")
         return out, hist
 
+    def query_stream(self, q, batch: int, mlp=None, thresh: float = 0.1, want_hist: bool = False):
+        """Streams a host batch through the device in sub-batches (DSLIM_SearchManager's
+        batch loop, dslim_query.cpp:160-420); returns (results, hist, learned log10 e)."""
+        n = q.nspec
+        out = np.zeros(n, dtype=L.RESULT_DTYPE)
+        hist = np.zeros((n, L.HC_HIST_BINS), dtype=np.uint32) if want_hist else None
+        learned = np.full(n, np.nan, dtype=np.float32) if mlp is not None else None
+        idx = np.ascontiguousarray(q.idx, dtype=np.uint32)
+        moz = np.ascontiguousarray(q.moz, dtype=np.uint32)
+        inten = np.ascontiguousarray(q.intensity, dtype=np.uint32)
+        prec = np.ascontiguousarray(q.precurse, dtype=np.float32)
+        dM = None if getattr(q, "dM", None) is None else np.ascontiguousarray(q.dM, dtype=np.float64)
+        self._check(self.lib.hc_dslim_query_stream(
+            self.ctx, L.ptr(idx), L.ptr(moz), L.ptr(inten), L.ptr(prec), L.ptr(dM), n, batch,
+            None if mlp is None else mlp.h, C.c_float(thresh), L.ptr(out), L.ptr(hist), L.ptr(learned)),
+            "hc_dslim_query_stream")
+        return out, hist, learned
+
     def query_device(self, d_idx: int, d_moz: int, d_int: int, d_prec: int, d_dM: int | None, nspec: int,
                      npeaks: int, d_out: int, d_hist: int, stream: int | None = None):
         """Device-buffer query (raw device pointers); enqueued on `stream`."""

@@ -321,6 +321,10 @@ def workload(name: str):
     if name == "open-500k":       # open-2m's shape at 1/4 of the database, 2,000 spectra (kernel profiles)
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 500000, 0xC14, 2000, 0xC15, {}
+    if name == "full-8m":         # 8M peptides + M-ox, 1M spectra of the mixed-window batch, streamed in 50k batches
+        p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+        return p, 8000000, 0xC40, 1000000, 0xC41, dict(
+            peaks=(20, 150), window_mix=[(0.5, "ppm", 10.0), (0.3, "da", 50.0), (0.2, "da", 500.0)])
     if name == "mixed-2m":        # open-2m index, 200k spectra, 20-150 peaks, mixed windows
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 2000000, 0xC10, 200000, 0xC21, dict(

@@ -232,6 +232,20 @@ int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, fl
  * measured against. Mode 0 is hc_mlp_evalues. */
 int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
                         float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
+/* ---- streaming query over a large host batch ----
+ * Replaces the batch loop of DSLIM_SearchManager (dslim_query.cpp:160-420),
+ * where an I/O thread fills QCHUNK-sized batches that DSLIM_QuerySpectrum
+ * searches one after another. The host batch (any host memory, CSR as in
+ * hc_dslim_query) is cut into sub-batches of `batch` spectra that alternate
+ * between two pinned/device staging slots, so the copies of one sub-batch
+ * overlap the search of the other. With `mlp` non-null the learned e-values
+ * (hc_mlp_evalues, `thresh`) are applied to every sub-batch and
+ * learned_log10e (optional, nspec floats) receives them. hist (optional)
+ * receives nspec*HC_HIST_BINS counts. Synchronous: returns when every result
+ * is in `out`. */
+int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uint32_t *moz, const uint32_t *intensity,
+                          const float *precurse, const double *dM, uint32_t nspec, uint32_t batch,
+                          hc_mlp *mlp, float thresh, hc_result *out, uint32_t *hist, float *learned_log10e);
 /* Diagnostics: with phase timing on, the search kernel adds up SM clock
  * cycles per phase (bucket setup, postings stream, score pass 1, score pass 2,
  * tile clear, rest) over all CTAs, then four counts (tiles, tiles scored by a
