@@ -40,7 +40,7 @@ namespace {
 //   chunk -> list map tile/2 (u16), past which a chunk finds its list by search.
 __host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 2; }
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
-constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two)
+constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two, >= 32 + 64)
 constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
 constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
@@ -153,7 +153,6 @@ struct SmemTail
     unsigned long long ph_last;
     unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations
     int2 win[HC_MAX_LENGTHS];  // the spectrum's window per length
-    uint32_t wsum[32];         // block scan
     float lgf[kLgTable];
 };
 
@@ -170,7 +169,7 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, cmap, defer, linfo, loff, pmoz, pint, wq, tail, total;
+    size_t qual, cmap, defer, linfo, lend, loff, pmoz, pint, wq, tail, total;
     uint32_t maxpairs, loffs;  // linfo / loff entries per buffer (two buffers each)
 };
 
@@ -184,7 +183,8 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     o.maxpairs = (uint32_t)maxpairs;
     o.loffs = (uint32_t)maxpairs + 4;
     o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
-    o.loff = o.linfo + 2 * 16 * maxpairs;
+    o.lend = o.linfo + 2 * 8 * maxpairs;  // (maxpairs = 100 (2 dF + 1): every size stays a multiple of 16)
+    o.loff = o.lend + 4 * maxpairs;
     o.pmoz = o.loff + 2 * 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
@@ -271,18 +271,12 @@ __device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, con
 }
 
 // Warp-level: exclusive chunk offsets of lists [0, np) in place (lo[np] =
-// total), linfo[i].z = offset; the total goes to *total and the postings
-// visited (4 bytes each) to *bytes. Must be called by all 32 lanes of a warp.
-__device__ void chunk_offsets(uint4 *linfo, uint32_t *lo, uint32_t np, int lane, uint32_t *total,
-                              unsigned long long *bytes)
+// total); the total also goes to *total. Must be called by all 32 lanes of a warp.
+__device__ void chunk_offsets(uint32_t *lo, uint32_t np, int lane, uint32_t *total)
 {
     const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
-    uint32_t sum = 0, post = 0;
-    for (uint32_t i = b; i < e; i++)
-    {
-        sum += lo[i];
-        post += linfo[i].y - linfo[i].x;
-    }
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += lo[i];
     uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
@@ -295,16 +289,13 @@ __device__ void chunk_offsets(uint4 *linfo, uint32_t *lo, uint32_t np, int lane,
     {
         const uint32_t t = lo[i];
         lo[i] = run;
-        linfo[i].z = run;
         run += t;
     }
-    post = __reduce_add_sync(0xFFFFFFFFu, post);
     if (lane == 31)
     {
         lo[np] = x;
         *total = x;
     }
-    if (lane == 0 && post) atomicAdd(bytes, 4ull * post);
 }
 
 // Asks L2 for the 128-byte lines holding postings [st, en) of qp (the 16-byte
@@ -379,7 +370,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     W *card = reinterpret_cast<W *>(smem);
     uint16_t *cmap = reinterpret_cast<uint16_t *>(smem + L.cmap);    // chunk -> list
     uint2 *defer = reinterpret_cast<uint2 *>(smem + L.defer);  // undecided candidates: {b word, y word}
-    uint4 *linfo = reinterpret_cast<uint4 *>(smem + L.linfo);  // per list: {first, end, chunk offset, intensity}
+    uint2 *linfo = reinterpret_cast<uint2 *>(smem + L.linfo);  // per list, two buffers: {first, intensity}
+    uint32_t *lend = reinterpret_cast<uint32_t *>(smem + L.lend);  // per list: end of the current job's list
     uint32_t *loff = reinterpret_cast<uint32_t *>(smem + L.loff);
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
@@ -542,24 +534,29 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         {
             // the first job's boundaries, directly
             const LenDev d = a.lens[jb.l];
+            uint32_t my_post = 0;
             for (uint32_t pr = tid; pr < np; pr += nthr)
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
                 const uint32_t st = row_lb(col, d.qp, jb.c0, d.qsh);
                 const uint32_t en = row_lb(col, d.qp, jb.c1, d.qsh);
-                linfo[pr] = make_uint4(st, en, 0u, pint[k]);
+                linfo[pr] = make_uint2(st, pint[k]);
+                lend[pr] = en;
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                my_post += en - st;
             }
+            my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
+            if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);  // postings visited
             __syncthreads();
-            if (wid == 0) chunk_offsets(linfo, loff, np, lane, &T.cchunks[0], &T.bytes);
+            if (wid == 0) chunk_offsets(loff, np, lane, &T.cchunks[0]);
         }
         __syncthreads();
         while (jb.l != kNoJob)
         {
             const LenDev d = a.lens[jb.l];
             const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
-            uint4 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
+            uint2 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
             uint32_t *lo_c = loff + cur * L.loffs, *lo_n = loff + (cur ^ 1) * L.loffs;
             const uint32_t C = T.cchunks[cur];
             // ---- chunk -> list map: each thread a contiguous run of chunks ----
@@ -641,13 +638,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                             if (kc < ccap) i = cmap[kc];
                             else
                                 while (i + 1 < np && lo_c[i + 1] <= kc) i++;
-                            const uint4 li = li_c[i];
+                            const uint2 li = li_c[i];
                             // a chunk never leaves its bucket (buckets start at
                             // multiples of 4, padded to them); its postings
                             // outside [first, end) belong to entries outside
                             // the tile and fail the index test below
-                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - li.z);
-                            inte[g] = li.w;
+                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - lo_c[i]);
+                            inte[g] = li.y;
                             v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
                         }
                     }
@@ -683,21 +680,24 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             // ---- the next job's list bounds, and its postings into L2 ----
             if (nj.l != kNoJob)
             {
+                uint32_t my_post = 0;
 #pragma unroll
                 for (int m = 0; m < kPf; m++)
                 {
                     const uint32_t pr = tid + m * nthr;
                     if (pr < np)
                     {
-                        const uint32_t st = same ? li_c[pr].y
+                        const uint32_t st = same ? lend[pr]
                                                  : (nj.c0 % kRowG == 0u
                                                         ? ps_lo[m]
                                                         : lower_bound_g(dn.qp, ps_lo[m], ps_hi[m], nj.c0 << (dn.qsh + 1)));
                         const uint32_t en = (nj.c1 % kRowG == 0u)
                                                 ? pf_lo[m]
                                                 : lower_bound_g(dn.qp, pf_lo[m], pf_hi[m], nj.c1 << (dn.qsh + 1));
-                        li_n[pr] = make_uint4(st, en, 0u, pint[pr / nbin]);
+                        li_n[pr] = make_uint2(st, pint[pr / nbin]);
+                        lend[pr] = en;
                         lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                        my_post += en - st;
                         prefetch_l2(dn.qp, st, en);
                     }
                 }
@@ -706,17 +706,21 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 {
                     const uint32_t k = pr / nbin, j = pr - k * nbin;
                     const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                    const uint32_t st = same ? li_c[pr].y : row_lb(col, dn.qp, nj.c0, dn.qsh);
+                    const uint32_t st = same ? lend[pr] : row_lb(col, dn.qp, nj.c0, dn.qsh);
                     const uint32_t en = row_lb(col, dn.qp, nj.c1, dn.qsh);
-                    li_n[pr] = make_uint4(st, en, 0u, pint[k]);
+                    li_n[pr] = make_uint2(st, pint[k]);
+                    lend[pr] = en;
                     lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                    my_post += en - st;
                     prefetch_l2(dn.qp, st, en);
                 }
+                my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
+                if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);  // postings visited
             }
             __syncthreads();
             HC_PHASE(1);
             // ---- the next job's chunk offsets (warp 0, before its scoring share) ----
-            if (wid == 0 && nj.l != kNoJob) chunk_offsets(li_n, lo_n, np, lane, &T.cchunks[cur ^ 1], &T.bytes);
+            if (wid == 0 && nj.l != kNoJob) chunk_offsets(lo_n, np, lane, &T.cchunks[cur ^ 1]);
             // ---- every candidate that reached min_shp ----
             // cpsms, histogram and the top hit (see score_one). The packed tile
             // is scanned two candidates per lane and step; a warp collects its

@@ -119,7 +119,7 @@ typedef struct hc_tuning
                               evaluation at the spectrum's end (<= HC_DEFER_MAX; 0: each
                               is evaluated in place). Results do not depend on it. */
 } hc_tuning;
-#define HC_DEFER_MAX 256
+#define HC_DEFER_MAX 128
 
 int hc_version(void);
 const char *hc_status_string(int status);

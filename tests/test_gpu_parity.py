@@ -121,7 +121,7 @@ def test_small_blocks(dslim, orc, threads, ppw):
     ix.close()
 
 
-@pytest.mark.parametrize("cap", [0, 1, 256])
+@pytest.mark.parametrize("cap", [0, 1, 128])
 def test_undecided_queue_capacity(dslim, orc, cap):
     """Candidates whose sign or histogram bin the float estimate leaves open:
     evaluated in place (cap 0), mostly in place once a one-entry queue is full,
