@@ -18,7 +18,8 @@ HC_MAX_MODS = 15
 
 STATUS = {0: "success", -3001: "invalid memory", -3002: "invalid parameter", -3003: "invalid index",
           -3004: "invalid size", -3007: "allocation failed", -3008: "invalid pointer",
-          -3010: "invalid modification", -3012: "not enough data", -3020: "CUDA error",
+          -3010: "invalid modification", -3012: "not enough data", -3006: "file not found",
+          -3013: "file error", -3020: "CUDA error",
           -3021: "device wait timed out", -3022: "no usable CUDA device"}
 
 ENTRY_DTYPE = np.dtype([("mass", "<f4"), ("seqid", "<u4"), ("sites", "<u8"),
@@ -84,6 +85,10 @@ _SIGS = [
                                     C.c_int64]),
     ("hc_dslim_query", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_dslim_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("hc_dslim_restore", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("hc_write_psms", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("hc_dslim_query_stream", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),

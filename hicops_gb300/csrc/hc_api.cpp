@@ -21,7 +21,7 @@ int cuda_check(hc_ctx *ctx, cudaError_t e, const char *what)
     return set_error(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_BAD_MEM_ALLOC : HC_ERR_CUDA, m);
 }
 
-static void free_len(LenHost &lh)
+void free_len(LenHost &lh)
 {
     cudaFree(lh.d_mass);
     cudaFree(lh.d_seqid);
@@ -78,6 +78,8 @@ const char *hc_status_string(int s)
     case HC_ERR_INVLD_PTR: return "invalid pointer";
     case HC_ERR_INVLD_MOD: return "invalid modification";
     case HC_ERR_NOT_ENOUGH_DATA: return "not enough data";
+    case HC_ERR_FILE_NOT_FOUND: return "file not found";
+    case HC_ERR_FILE_ERROR: return "file error";
     case HC_ERR_CUDA: return "CUDA error";
     case HC_ERR_TIMEOUT: return "device wait timed out";
     case HC_ERR_NO_DEVICE: return "no usable CUDA device";

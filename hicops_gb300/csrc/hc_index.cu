@@ -13,6 +13,7 @@
 #include <cstdio>
 
 #include <algorithm>
+#include <vector>
 
 #include "hc_internal.h"
 
@@ -397,6 +398,19 @@ __global__ void k_qpost(const uint32_t *__restrict__ bA, const uint32_t *__restr
     }
 }
 
+// counts query-posting words that are neither padding nor an (entry < n, ion < speclen) pair
+__global__ void k_check_qpost(const uint32_t *__restrict__ qp, size_t total, uint32_t n, uint32_t qsh,
+                              uint32_t speclen, uint32_t *__restrict__ bad)
+{
+    uint32_t b = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t x = qp[i];
+        if (x != kQpostPad && ((x >> (qsh + 1)) >= n || (x & ((1u << qsh) - 1u)) >= speclen)) b++;
+    }
+    if (b) atomicAdd(bad, b);
+}
+
 // query postings -> ids (the reference's iA), one thread per bucket
 __global__ void k_qpost_ids(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ qA,
                             const uint32_t *__restrict__ qp, uint32_t nb, uint32_t speclen, uint32_t qsh,
@@ -575,13 +589,58 @@ int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_qp, 0xFF, 4 * ((size_t)total + kIaPad), st));
     if (d_ids && lh.npost)
         k_qpost<<<bblocks, 256, 0, st>>>(lh.d_bA, d_ids, lh.d_qA, nb, speclen, speclen / 2, qsh, lh.d_qp);
+    HC_CUDA(ctx, cudaGetLastError());
+    return build_rows(ctx, lh);
+}
+
+// The row table of a length from its query postings (qA, qp, qsh, n set).
+int build_rows(hc_ctx *ctx, LenHost &lh)
+{
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    cudaFree(lh.d_rows);
+    lh.d_rows = nullptr;
     lh.stride = (lh.n + kRowG - 1) / kRowG + 1;
     HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
     const uint64_t rt = (uint64_t)nb * lh.stride;
     const unsigned blocks = (unsigned)std::min<uint64_t>((rt + 255) / 256, (uint64_t)ctx->sm_count * 64);
-    k_row_table<<<blocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, qsh, lh.d_rows);
+    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, lh.qsh, lh.d_rows);
     HC_CUDA(ctx, cudaGetLastError());
-    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HC_SUCCESS;
+}
+
+// Checks query postings read from outside (an index file): bucket starts
+// ascending multiples of 4 ending at the total, and every word padding or a
+// valid (entry, ion). Returns HC_ERR_FILE_ERROR otherwise.
+int check_query_postings(hc_ctx *ctx, const LenHost &lh, uint64_t qtotal)
+{
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
+    uint32_t q = 0;
+    while ((1u << q) < speclen) q++;
+    if (lh.qsh != q || lh.n + 2ull > (1ull << (31 - q)))
+        return set_error(ctx, HC_ERR_FILE_ERROR, "index file: postings layout does not match the parameters");
+    std::vector<uint32_t> qa(nb + 1);
+    HC_CUDA(ctx, cudaMemcpy(qa.data(), lh.d_qA, 4ull * (nb + 1), cudaMemcpyDeviceToHost));
+    for (uint32_t b = 0; b <= nb; b++)
+        if ((qa[b] & 3u) || (b && qa[b] < qa[b - 1]))
+            return set_error(ctx, HC_ERR_FILE_ERROR, "index file: bucket starts out of order");
+    if (qa[0] != 0 || qa[nb] != qtotal) return set_error(ctx, HC_ERR_FILE_ERROR, "index file: bucket starts");
+    uint32_t *d_bad = nullptr;
+    HC_CUDA(ctx, cudaMalloc((void **)&d_bad, 4));
+    uint32_t bad = 0;
+    cudaError_t e = cudaMemset(d_bad, 0, 4);
+    if (e == cudaSuccess && qtotal)
+    {
+        const unsigned blocks = (unsigned)std::min<uint64_t>((qtotal + 255) / 256, (uint64_t)ctx->sm_count * 32);
+        k_check_qpost<<<blocks, 256, 0, ctx->stream>>>(lh.d_qp, qtotal, lh.n, lh.qsh, speclen, d_bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&bad, d_bad, 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    HC_CUDA(ctx, e);
+    if (bad) return set_error(ctx, HC_ERR_FILE_ERROR, "index file: invalid postings");
     return HC_SUCCESS;
 }
 

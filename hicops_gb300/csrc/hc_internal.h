@@ -178,6 +178,9 @@ void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
 // hc_index.cu
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
 int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids);
+int build_rows(hc_ctx *ctx, LenHost &lh);
+int check_query_postings(hc_ctx *ctx, const LenHost &lh, uint64_t qtotal);
+void free_len(LenHost &lh);
 int export_ids(hc_ctx *ctx, const LenHost &lh, uint32_t *d_ids);
 
 // hc_query.cu

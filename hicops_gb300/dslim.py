@@ -118,6 +118,27 @@ class Index:
                                             L.ptr(dM), n, L.ptr(out), L.ptr(hist)), "hc_dslim_query")
         return out, hist
 
+    def save(self, path: str):
+        """Writes the built lengths to an index file (hc_dslim_save)."""
+        self._check(self.lib.hc_dslim_save(self.ctx, path.encode()), "hc_dslim_save")
+
+    def restore(self, path: str, seqs: dict | None = None):
+        """Reads an index file written with the same index parameters (hc_dslim_restore)."""
+        self._check(self.lib.hc_dslim_restore(self.ctx, path.encode()), "hc_dslim_restore")
+        if seqs is not None:
+            self.seqs.update(seqs)
+
+    def write_psms(self, path: str, res: np.ndarray, q, file_label: str = "", spec_base: int = 0,
+                   append: bool = False):
+        """DFile_PrintScore's TSV (dslim_fileout.cpp:112-152) for the reported spectra of `res`."""
+        res = np.ascontiguousarray(res, dtype=L.RESULT_DTYPE)
+        prec = np.ascontiguousarray(q.precurse, dtype=np.float32)
+        chg = None if q.charges is None else np.ascontiguousarray(q.charges, dtype=np.int32)
+        rt = None if q.rtimes is None else np.ascontiguousarray(q.rtimes, dtype=np.float32)
+        self._check(self.lib.hc_write_psms(self.ctx, path.encode(), file_label.encode(), spec_base, L.ptr(res),
+                                           res.shape[0], L.ptr(prec), L.ptr(chg), L.ptr(rt), int(append)),
+                    "hc_write_psms")
+
     def query_stream(self, q, batch: int, mlp=None, thresh: float = 0.1, want_hist: bool = False):
         """Streams a host batch through the device in sub-batches (DSLIM_SearchManager's
         batch loop, dslim_query.cpp:160-420); returns (results, hist, learned log10 e)."""

@@ -121,9 +121,9 @@ def make_database(n_peptides: int, seed: int, params: SearchParams) -> dict[int,
     db = {L: np.array(v, dtype=np.uint8).reshape(-1, L) for L, v in out.items()}
     order = sorted(db, key=lambda L: -db[L].shape[0])
     i = 0
-    while excess > 0:
+    while excess > 0:  # total >= n_peptides, so this ends (a length may become empty)
         L = order[i % len(order)]
-        if db[L].shape[0] > 1:
+        if db[L].shape[0] > 0:
             db[L] = db[L][:-1]
             excess -= 1
         i += 1

@@ -35,10 +35,12 @@ extern "C" {
 #define HC_ERR_INVLD_PARAM (-3002)
 #define HC_ERR_INVLD_INDEX (-3003)
 #define HC_ERR_INVLD_SIZE (-3004)
+#define HC_ERR_FILE_NOT_FOUND (-3006)
 #define HC_ERR_BAD_MEM_ALLOC (-3007)
 #define HC_ERR_INVLD_PTR (-3008)
 #define HC_ERR_INVLD_MOD (-3010)
 #define HC_ERR_NOT_ENOUGH_DATA (-3012)
+#define HC_ERR_FILE_ERROR (-3013)
 /* codes without a reference counterpart */
 #define HC_ERR_CUDA (-3020)      /* a CUDA runtime call failed; see hc_last_error */
 #define HC_ERR_TIMEOUT (-3021)   /* a bounded device wait ran out */
@@ -232,6 +234,27 @@ int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, fl
  * measured against. Mode 0 is hc_mlp_evalues. */
 int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
                         float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
+/* ---- on-disk index (no reference counterpart: the reference rebuilds its
+ * index on every run, hicops.cpp:174-260) ----
+ * hc_dslim_save writes every built length (entries, sequences, bucket offsets
+ * and the device postings) to one file with a hash of the index-defining
+ * parameters; hc_dslim_restore reads it into a context created with the same
+ * parameters (else HC_ERR_INVLD_PARAM) and rebuilds the derived row tables.
+ * HC_ERR_FILE_NOT_FOUND / HC_ERR_FILE_ERROR on I/O failures. */
+int hc_dslim_save(hc_ctx *ctx, const char *path);
+int hc_dslim_restore(hc_ctx *ctx, const char *path);
+
+/* ---- PSM output (DFile_PrintScore, dslim_fileout.cpp:112-152; header 68-72) ----
+ * Writes one TSV row per reported spectrum (reported != 0) with the
+ * reference's columns: file, scan_num (spec_base + i + 1), prec_mass, charge,
+ * retention_time, peptide, matched_ions, total_ions, calc_pep_mass, mass_diff,
+ * mod_info (empty, as in the reference), hyperscore, expectscore, num_hits;
+ * numbers as std::to_string prints them. The header is written unless
+ * `append`. charges / rtimes may be NULL (printed as 0). */
+int hc_write_psms(hc_ctx *ctx, const char *path, const char *file_label, uint32_t spec_base,
+                  const hc_result *res, uint32_t nspec, const float *precurse, const int32_t *charges,
+                  const float *rtimes, int append);
+
 /* ---- streaming query over a large host batch ----
  * Replaces the batch loop of DSLIM_SearchManager (dslim_query.cpp:160-420),
  * where an I/O thread fills QCHUNK-sized batches that DSLIM_QuerySpectrum
