@@ -14,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libhicops_gb300.so")
 
 HC_HIST_BINS = 1002
+HC_QALEN = 100
 HC_MAX_MODS = 15
 
 STATUS = {0: "success", -3001: "invalid memory", -3002: "invalid parameter", -3003: "invalid index",
@@ -89,6 +90,12 @@ _SIGS = [
     ("hc_dslim_restore", C.c_int, [C.c_void_p, C.c_char_p]),
     ("hc_write_psms", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("hc_ms2_open", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint32),
+                              C.POINTER(C.c_uint32)]),
+    ("hc_ms2_extract", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32),
+                                 C.POINTER(C.c_uint64)]),
+    ("hc_ms2_close", C.c_int, [C.c_void_p]),
     ("hc_dslim_query_stream", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),

@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libhicops_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU = ["hc_index.cu", "hc_query.cu", "hc_mlp.cu", "hc_noalloc.cu", "hc_output.cu"]
+CU = ["hc_index.cu", "hc_query.cu", "hc_mlp.cu", "hc_noalloc.cu", "hc_output.cu", "hc_ms2.cu"]
 CPP = ["hc_api.cpp", "hc_host.cpp", "hc_batch.cpp", "hc_stream.cpp", "hc_store.cpp"]
 
 

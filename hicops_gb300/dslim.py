@@ -193,6 +193,68 @@ class Index:
         return sid, mod, site
 
 
+class MSQuery:
+    """MS2 file reader with device peak picking: the reference's MSQuery
+    (source/core/include/msquery.hpp:73-113). ``initialize`` reads the file
+    (hc_ms2_open), ``extractbatch`` returns the next batch of at most `count`
+    picked spectra as a Queries-layout batch (hc_ms2_extract)."""
+
+    def __init__(self, index: Index):
+        self.ix = index
+        self.h = None
+        self.QAcount = 0
+        self.maxslen = 0
+        self.running_count = 0
+
+    def initialize(self, path: str):
+        h = C.c_void_p()
+        n, mx = C.c_uint32(), C.c_uint32()
+        self.ix._check(self.ix.lib.hc_ms2_open(self.ix.ctx, path.encode(), C.byref(h), C.byref(n), C.byref(mx)),
+                       "hc_ms2_open")
+        self.DeinitQueryFile()
+        self.h, self.QAcount, self.maxslen, self.running_count = h, n.value, mx.value, 0
+        return self
+
+    def getQAcount(self) -> int:
+        return self.QAcount
+
+    def extract(self, first: int, count: int):
+        """Spectra [first, first+count) (clamped) as a QueryBatch."""
+        from .synthetic import QueryBatch
+        count = max(0, min(count, self.QAcount - first))
+        idx = np.zeros(count + 1, dtype=np.uint32)
+        moz = np.zeros(max(count * L.HC_QALEN, 1), dtype=np.uint32)
+        inten = np.zeros_like(moz)
+        prec = np.zeros(count, dtype=np.float32)
+        chg = np.zeros(count, dtype=np.int32)
+        rt = np.zeros(count, dtype=np.float32)
+        nout, npk = C.c_uint32(), C.c_uint64()
+        self.ix._check(self.ix.lib.hc_ms2_extract(self.ix.ctx, self.h, first, count, L.ptr(idx), L.ptr(moz),
+                                                  L.ptr(inten), L.ptr(prec), L.ptr(chg), L.ptr(rt),
+                                                  C.byref(nout), C.byref(npk)), "hc_ms2_extract")
+        k = int(npk.value)
+        return QueryBatch(idx=idx, moz=moz[:k].copy(), intensity=inten[:k].copy(), precurse=prec, charges=chg,
+                          rtimes=rt)
+
+    def extractbatch(self, count: int):
+        """The next batch and the number of spectra left (MSQuery::extractbatch, msquery.cpp:239-297)."""
+        b = self.extract(self.running_count, count)
+        self.running_count += b.nspec
+        return b, self.QAcount - self.running_count
+
+    def DeinitQueryFile(self):
+        if self.h:
+            self.ix.lib.hc_ms2_close(self.h)
+            self.h = None
+        self.QAcount = self.running_count = self.maxslen = 0
+
+    def __del__(self):
+        try:
+            self.DeinitQueryFile()
+        except Exception:
+            pass
+
+
 def DSLIM_Construct(index: Index, L_: int, seqs: np.ndarray) -> int:
     """dslim.h:49 — build one length's index on the device; returns SLM_SUCCESS."""
     index.construct(L_, seqs)

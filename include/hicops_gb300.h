@@ -255,6 +255,33 @@ int hc_write_psms(hc_ctx *ctx, const char *path, const char *file_label, uint32_
                   const hc_result *res, uint32_t nspec, const float *precurse, const int32_t *charges,
                   const float *rtimes, int append);
 
+/* ---- MS2 ingestion (MSQuery, source/core/msquery.cpp) ----
+ * hc_ms2_open replaces MSQuery::initialize (msquery.cpp:88-178) and reads the
+ * whole file once as MSQuery::readspectrum reads it spectrum by spectrum
+ * (msquery.cpp:300-505): one spectrum per 'S' line; 'Z' lines give the charge
+ * and precursor, 'I RTime' lines the retention time, every other non-empty
+ * line not starting with 'H' or 'D' a peak, m/z scaled by the context's
+ * `scale` and intensity by 1000, truncated to integers. *nspec = number of
+ * spectra, *maxslen = largest raw peak count. HC_ERR_FILE_ERROR when the file
+ * cannot be opened or read, HC_ERR_INVLD_SIZE when it holds no peak at all
+ * (the reference's ERR_INVLD_SIZE). */
+typedef struct hc_ms2 hc_ms2;
+int hc_ms2_open(hc_ctx *ctx, const char *path, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen);
+/* Replaces MSQuery::extractbatch (msquery.cpp:239-297) and pickpeaks
+ * (msquery.cpp:509-569): spectra [first, first+count) clamped to the file's
+ * end (*nout = how many) are peak-picked on the device (quicksort by
+ * intensity with the reference's tie order, top peak = base_int, at most
+ * HC_QALEN kept, those >= min_int) into the CSR batch idx[*nout+1],
+ * moz / intensity (room for *nout * HC_QALEN each), precurse, charges
+ * (MAX(1, Z)), rtimes (MAX(0, rtime)); *npeaks = idx[*nout]. The batch
+ * layout is the reference's Queries (slm_dsts.h:422-559), ready for
+ * hc_dslim_query. */
+int hc_ms2_extract(hc_ctx *ctx, hc_ms2 *m, uint32_t first, uint32_t count, uint32_t *idx, uint32_t *moz,
+                   uint32_t *intensity, float *precurse, int32_t *charges, float *rtimes, uint32_t *nout,
+                   uint64_t *npeaks);
+/* Replaces MSQuery::DeinitQueryFile (msquery.cpp:571-605). */
+int hc_ms2_close(hc_ms2 *m);
+
 /* ---- streaming query over a large host batch ----
  * Replaces the batch loop of DSLIM_SearchManager (dslim_query.cpp:160-420),
  * where an I/O thread fills QCHUNK-sized batches that DSLIM_QuerySpectrum

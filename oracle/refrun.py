@@ -76,3 +76,34 @@ def run(params, db: dict, queries, dump_index: bool = False, workdir: str | None
             d["iA"] = np.fromfile(p + "_iA.bin", dtype=np.uint32)
         res["lengths"][L] = d
     return res
+
+
+MS2_DRIVER = os.path.join(HERE, "_ref", "ms2_driver")
+
+
+def ms2_available() -> bool:
+    return os.path.exists(MS2_DRIVER)
+
+
+def run_ms2(path: str, scale: int, base_int: int, min_int: int):
+    """The reference MS2 reader + pickpeaks on one file (oracle/ref/ms2_driver.cpp):
+    (status, dict of idx, moz, intensity, precurse, charges, rtimes)."""
+    fd, out = tempfile.mkstemp(prefix="hcms2_", suffix=".bin")
+    os.close(fd)
+    try:
+        r = subprocess.run([MS2_DRIVER, path, str(scale), str(base_int), str(min_int), out],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"ms2_driver failed ({r.returncode}): {r.stderr[-2000:]}")
+        d = np.fromfile(out, dtype="<u4")
+    finally:
+        os.unlink(out)
+    st = int(d[:1].view("<i4")[0])
+    n, npk = int(d[1]), int(d[2])
+    o = 3
+    res = {}
+    for k, cnt, dt in (("idx", n + 1, "<u4"), ("moz", npk, "<u4"), ("intensity", npk, "<u4"),
+                       ("precurse", n, "<f4"), ("charges", n, "<i4"), ("rtimes", n, "<f4")):
+        res[k] = d[o:o + cnt].view(dt).copy()
+        o += cnt
+    return st, res
