@@ -227,22 +227,12 @@ int hc_dslim_construct(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t np
     free_len(*lh);
     int rc = upload_seqs(ctx, *lh, seqs, npep);
     if (rc) return rc;
-    std::vector<hc_entry> ents;
-    if (order)
-    {
-        for (uint32_t i = 0; i < norder; i++)
-            if (order[i].seqid >= npep) return set_error(ctx, HC_ERR_INVLD_INDEX, "entry seqid out of range");
-        ents.assign(order, order + norder);
-    }
-    else
-    {
-        int64_t n = make_entries(ctx->p, L, seqs, npep, nullptr, 0);
-        ents.resize((size_t)n);
-        make_entries(ctx->p, L, seqs, npep, ents.data(), n);
-    }
-    if (ents.size() >= (1u << 24)) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^24 entries in one length");
-    lh->n = (uint32_t)ents.size();
-    return build_length_device(ctx, *lh, ents.data(), order == nullptr);
+    if (!order) return build_length_device(ctx, *lh, nullptr, true);  // entries enumerated on the device
+    for (uint32_t i = 0; i < norder; i++)
+        if (order[i].seqid >= npep) return set_error(ctx, HC_ERR_INVLD_INDEX, "entry seqid out of range");
+    if (norder >= (1u << 24)) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^24 entries in one length");
+    lh->n = norder;
+    return build_length_device(ctx, *lh, order, false);
 }
 
 int hc_dslim_load(hc_ctx *ctx, uint32_t L, const uint8_t *seqs, uint32_t npep, const hc_entry *entries,

@@ -107,6 +107,31 @@ struct VariantGen
 
 }  // namespace
 
+void make_enum_const(const hc_params &p, EnumConst *e)
+{
+    std::memset(e, 0, sizeof(*e));
+    for (int a = 0; a < 26; a++)
+    {
+        e->aa[a] = kAAMass[a];
+        e->stat[a] = kStatMods[a];
+        e->cond_of[a] = -1;
+    }
+    e->h2o = kH2O;
+    const uint32_t nm = p.nmods < HC_MAX_MODS ? p.nmods : HC_MAX_MODS;
+    for (uint32_t m = 0; m < nm; m++)
+    {
+        for (int j = 0; j < 4 && p.mod_res[m][j]; j++)
+        {
+            const int c = p.mod_res[m][j] - 'A';
+            if (c >= 0 && c < 26) e->cond_of[c] = (int8_t)m;
+        }
+        e->limit[m] = p.mod_per_pep[m];
+        e->modadd[m] = (float)p.mod_mass[m] / (float)p.scale;
+    }
+    e->nmods = nm;
+    e->vmods = p.vmods_per_pep;
+}
+
 void make_ion_tables(const hc_params &p, IonTables *t)
 {
     std::memset(t, 0, sizeof(*t));

@@ -1,5 +1,8 @@
 // Device construction of the SLM index of one peptide length
 // (DSLIM_Construct, source/core/dslim.cpp:46-138):
+//   0. entries (base peptides, then their variable-mod variants) enumerated
+//      on the device (LBE_GeneratePeps, lbe_internal.cpp:204-229, and
+//      MODS_GenerateMods, mods.cpp:448-496),
 //   1. entries sorted by mass on the device (stable LSD radix sort; the
 //      reference uses std::sort, lbe_internal.cpp:184-187),
 //   2. ion keys of every entry from integer tables (UTILS_GenerateSpectrum /
@@ -228,6 +231,97 @@ cudaError_t radix_sort(uint32_t *keys0, uint32_t *keys1, uint32_t *vals0, uint32
 
 // ---- entries ---------------------------------------------------------------
 
+// Entry enumeration on the device, one thread per peptide. The base entry of
+// peptide i (LBE_GeneratePeps, lbe_internal.cpp:204-229) is entry i; its
+// variable-mod variants (MODS_GenerateMods, mods.cpp:448-496) follow all base
+// entries, peptide by peptide, in the order of MODS_ModList's depth-first walk
+// (mods.cpp:333-384): at each modifiable position the branch that modifies it
+// comes before the one that skips it, and a variant is emitted as each mod is
+// added. Here the walk is a loop over a stack of chosen positions. The first
+// pass (out == nullptr) counts the variants per peptide; the second writes
+// them at npep + voff[i].
+__global__ void k_enum_entries(const uint8_t *__restrict__ seqs, uint32_t L, uint32_t npep, EnumConst ec,
+                               const uint32_t *__restrict__ voff, uint32_t *__restrict__ vcount,
+                               float *__restrict__ mass, uint32_t *__restrict__ seqid,
+                               uint64_t *__restrict__ sites, uint32_t *__restrict__ modnum)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npep) return;
+    const uint8_t *s = seqs + (size_t)i * L;
+    // UTILS_CalculatePepMass: two float additions per residue, in order
+    float pm = ec.h2o;
+    for (uint32_t l = 0; l < L; l++)
+    {
+        pm += ec.aa[s[l] - 'A'];
+        pm += ec.stat[s[l] - 'A'];
+    }
+    const bool write = voff != nullptr;
+    if (write)
+    {
+        mass[i] = pm;
+        seqid[i] = i;
+        sites[i] = 0;
+        modnum[i] = 0;
+    }
+    uint32_t k = 0;
+    if (ec.vmods > 0 && ec.nmods > 0)
+    {
+        int cap[HC_MAX_MODS];
+        for (int m = 0; m < HC_MAX_MODS; m++) cap[m] = (int)ec.limit[m];
+        uint8_t pos[64];
+        uint32_t d = 0, mn = 0;
+        uint64_t st = 0;
+        uint32_t start = 0;
+        const uint64_t at = write ? (uint64_t)npep + voff[i] : 0;
+        for (;;)
+        {
+            int p = -1;
+            if (d < ec.vmods && d < 64)
+                for (uint32_t q = start; q < L; q++)
+                {
+                    const int c = ec.cond_of[s[q] - 'A'];
+                    if (c >= 0 && cap[c] > 0)
+                    {
+                        p = (int)q;
+                        break;
+                    }
+                }
+            if (p >= 0)
+            {
+                const int c = ec.cond_of[s[p] - 'A'];
+                cap[c] -= 1;
+                pos[d] = (uint8_t)p;
+                mn += (1u << ((4u * d) & 31u)) * (uint32_t)(1 + c);  // shift count taken mod 32, as the CPU does
+                st |= 1ull << p;
+                d++;
+                if (write)
+                {
+                    // UTILS_CalculateModMass: only the first mod's mass is added
+                    const uint64_t e = at + k;
+                    mass[e] = pm + ec.modadd[(mn & 0xF) - 1];
+                    seqid[e] = i;
+                    sites[e] = st;
+                    modnum[e] = mn;
+                }
+                k++;
+                start = (uint32_t)p + 1;
+            }
+            else
+            {
+                if (d == 0) break;
+                d--;
+                const uint32_t q = pos[d];
+                const int c = ec.cond_of[s[q] - 'A'];
+                cap[c] += 1;
+                mn -= (1u << ((4u * d) & 31u)) * (uint32_t)(1 + c);
+                st &= ~(1ull << q);
+                start = q + 1;
+            }
+        }
+    }
+    if (!write) vcount[i] = k;
+}
+
 __global__ void k_mass_keys(const float *__restrict__ mass, uint32_t n, uint32_t *__restrict__ keys)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -435,30 +529,101 @@ cudaError_t dalloc(T **p, size_t n)
 
 }  // namespace
 
+// The entries of one length enumerated on the device (k_enum_entries, two
+// passes around a scan of the per-peptide variant counts) into fresh SoA
+// arrays in generation order; sets lh.n.
+static int enumerate_entries(hc_ctx *ctx, LenHost &lh, float **d_m, uint32_t **d_s, uint64_t **d_si,
+                             uint32_t **d_mo, int *launches)
+{
+    cudaStream_t st = ctx->stream;
+    const uint32_t npep = lh.npep, L = lh.L;
+    EnumConst ec;
+    make_enum_const(ctx->p, &ec);
+    uint32_t *cnt = nullptr, *stmp = nullptr;
+    HC_CUDA(ctx, dalloc(&cnt, (size_t)npep + 1));
+    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words((size_t)npep + 1)));
+    HC_CUDA(ctx, cudaMemsetAsync(cnt, 0, 4ull * (npep + 1), st));
+    const unsigned grid = (npep + 127) / 128;
+    if (npep)
+    {
+        k_enum_entries<<<grid, 128, 0, st>>>(lh.d_seqs, L, npep, ec, nullptr, cnt, nullptr, nullptr, nullptr,
+                                              nullptr);
+        (*launches)++;
+    }
+    HC_CUDA(ctx, scan_exclusive(cnt, (size_t)npep + 1, stmp, st));
+    uint32_t nvar = 0;
+    HC_CUDA(ctx, cudaMemcpyAsync(&nvar, cnt + npep, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    const uint64_t n = (uint64_t)npep + nvar;
+    if (n >= (1u << 24))
+    {
+        cudaFree(cnt);
+        cudaFree(stmp);
+        return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^24 entries in one length");
+    }
+    lh.n = (uint32_t)n;
+    HC_CUDA(ctx, dalloc(d_m, n));
+    HC_CUDA(ctx, dalloc(d_s, n));
+    HC_CUDA(ctx, dalloc(d_si, n));
+    HC_CUDA(ctx, dalloc(d_mo, n));
+    if (npep)
+    {
+        k_enum_entries<<<grid, 128, 0, st>>>(lh.d_seqs, L, npep, ec, cnt, nullptr, *d_m, *d_s, *d_si, *d_mo);
+        (*launches)++;
+    }
+    HC_CUDA(ctx, cudaGetLastError());
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    cudaFree(cnt);
+    cudaFree(stmp);
+    return HC_SUCCESS;
+}
+
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass)
 {
     cudaStream_t st = ctx->stream;
+    int launches = 0;
+    // entries in generation order: enumerated here, or uploaded from the host
+    float *d_m0 = nullptr;
+    uint32_t *d_s0 = nullptr, *d_mod0 = nullptr;
+    uint64_t *d_site0 = nullptr;
+    if (!h_entries)
+    {
+        const int rc = enumerate_entries(ctx, lh, &d_m0, &d_s0, &d_site0, &d_mod0, &launches);
+        if (rc) return rc;
+    }
     const uint32_t n = lh.n, L = lh.L;
     const uint32_t speclen = 2 * ctx->p.maxz * (L - 1);
     const size_t M = (size_t)n * speclen;
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
-    int launches = 0;
-    if (M >= 0x80000000ull) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^31 ions in one length");
-
-    // entries: upload in SoA, sort by mass (or keep the given order)
-    std::vector<float> hm(n);
-    std::vector<uint32_t> hs(n), hmod(n);
-    std::vector<uint64_t> hsite(n);
-    for (uint32_t i = 0; i < n; i++)
+    if (M >= 0x80000000ull)
     {
-        hm[i] = h_entries[i].mass;
-        hs[i] = h_entries[i].seqid;
-        hsite[i] = h_entries[i].sites;
-        hmod[i] = h_entries[i].modnum;
+        cudaFree(d_m0);
+        cudaFree(d_s0);
+        cudaFree(d_mod0);
+        cudaFree(d_site0);
+        return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^31 ions in one length");
     }
-    float *d_m0 = nullptr;
-    uint32_t *d_s0 = nullptr, *d_mod0 = nullptr;
-    uint64_t *d_site0 = nullptr;
+    if (h_entries && (sort_by_mass && n > 1))
+    {
+        std::vector<float> hm(n);
+        std::vector<uint32_t> hs(n), hmod(n);
+        std::vector<uint64_t> hsite(n);
+        for (uint32_t i = 0; i < n; i++)
+        {
+            hm[i] = h_entries[i].mass;
+            hs[i] = h_entries[i].seqid;
+            hsite[i] = h_entries[i].sites;
+            hmod[i] = h_entries[i].modnum;
+        }
+        HC_CUDA(ctx, dalloc(&d_m0, n));
+        HC_CUDA(ctx, dalloc(&d_s0, n));
+        HC_CUDA(ctx, dalloc(&d_mod0, n));
+        HC_CUDA(ctx, dalloc(&d_site0, n));
+        HC_CUDA(ctx, cudaMemcpy(d_m0, hm.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(d_s0, hs.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(d_mod0, hmod.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(d_site0, hsite.data(), 8ull * n, cudaMemcpyHostToDevice));
+    }
     HC_CUDA(ctx, dalloc(&lh.d_mass, n));
     HC_CUDA(ctx, dalloc(&lh.d_seqid, n));
     HC_CUDA(ctx, dalloc(&lh.d_sites, n));
@@ -480,14 +645,6 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
 
     if (sort_by_mass && n > 1)
     {
-        HC_CUDA(ctx, dalloc(&d_m0, n));
-        HC_CUDA(ctx, dalloc(&d_s0, n));
-        HC_CUDA(ctx, dalloc(&d_mod0, n));
-        HC_CUDA(ctx, dalloc(&d_site0, n));
-        HC_CUDA(ctx, cudaMemcpyAsync(d_m0, hm.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(d_s0, hs.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(d_mod0, hmod.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(d_site0, hsite.data(), 8ull * n, cudaMemcpyHostToDevice, st));
         k_mass_keys<<<(n + 255) / 256, 256, 0, st>>>(d_m0, n, k0);
         int which = 0;
         HC_CUDA(ctx, radix_sort(k0, k1, v0, v1, n, 32, hist, stmp, st, &which, &launches, false, true));
@@ -498,12 +655,29 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
                                                           lh.d_modnum);
         launches += 2;
     }
+    else if (d_m0)
+    {
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_mass, d_m0, 4ull * n, cudaMemcpyDeviceToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_seqid, d_s0, 4ull * n, cudaMemcpyDeviceToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_modnum, d_mod0, 4ull * n, cudaMemcpyDeviceToDevice, st));
+        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_sites, d_site0, 8ull * n, cudaMemcpyDeviceToDevice, st));
+    }
     else
     {
-        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_mass, hm.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_seqid, hs.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_modnum, hmod.data(), 4ull * n, cudaMemcpyHostToDevice, st));
-        HC_CUDA(ctx, cudaMemcpyAsync(lh.d_sites, hsite.data(), 8ull * n, cudaMemcpyHostToDevice, st));
+        std::vector<float> hm(n);
+        std::vector<uint32_t> hs(n), hmod(n);
+        std::vector<uint64_t> hsite(n);
+        for (uint32_t i = 0; i < n; i++)
+        {
+            hm[i] = h_entries[i].mass;
+            hs[i] = h_entries[i].seqid;
+            hsite[i] = h_entries[i].sites;
+            hmod[i] = h_entries[i].modnum;
+        }
+        HC_CUDA(ctx, cudaMemcpy(lh.d_mass, hm.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(lh.d_seqid, hs.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(lh.d_modnum, hmod.data(), 4ull * n, cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(lh.d_sites, hsite.data(), 8ull * n, cudaMemcpyHostToDevice));
     }
 
     // ion keys -> (k0), sorted with ids -> iA, bucket bounds -> bA

@@ -167,7 +167,24 @@ struct hc_ctx
 
 namespace hc {
 
+// What the device entry enumeration needs (passed by value to its kernels):
+// the float residue and static-mod masses of UTILS_CalculatePepMass
+// (utils.cpp:290-303), the residue -> mod-condition map and per-condition
+// limits of MODS_ModList (mods.cpp:333-384), and each mod's mass as
+// UTILS_CalculateModMass adds it (float(scaled mass) / float(scale)).
+struct EnumConst
+{
+    float aa[26];
+    float stat[26];
+    float h2o;
+    int8_t cond_of[26];  // mod condition of a residue, -1 if none
+    uint32_t limit[HC_MAX_MODS];
+    float modadd[HC_MAX_MODS];
+    uint32_t vmods, nmods;
+};
+
 // hc_host.cpp
+void make_enum_const(const hc_params &p, EnumConst *e);
 void make_ion_tables(const hc_params &p, IonTables *t);
 void make_query_const(QueryConst *q);
 void make_log10_table(double *t, uint32_t n);

@@ -42,6 +42,26 @@ def test_index_bitexact(dslim, orc, name, npep, nq, seed):
     ix.close()
 
 
+@pytest.mark.parametrize("mods,vmods", [([("M", 15.99, 2), ("STY", 79.97, 1)], 3),
+                                         ([("M", 15.99, 1), ("NQ", 0.98, 2), ("STY", 79.97, 3)], 4),
+                                         ([("M", 15.99, 3)], 1)])
+def test_device_enumeration_multi_mod(dslim, orc, mods, vmods):
+    """Entries enumerated on the device (several mod conditions, per-condition
+    limits, a total limit) equal the host enumeration, sorted stably by mass."""
+    p = S.SearchParams(maxz=2, dF=1, dM=100.0, vmods_per_pep=vmods, mods=mods)
+    db = S.make_database(4000, 77 + vmods, p)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    nvar = 0
+    for L in range(p.min_len, p.max_len + 1):
+        e = ix.entries(L)
+        oe = orc.make_entries(db[L], L, p)
+        assert np.array_equal(e.view(np.uint8), oe.view(np.uint8)), f"entries differ at L={L}"
+        nvar += int((oe["modnum"] != 0).sum())
+    assert nvar > 1000
+    ix.close()
+
+
 @pytest.mark.parametrize("name,npep,nq,seed", [("plain", 3000, 400, 303), ("mods", 3000, 400, 404)])
 def test_query_parity(dslim, orc, name, npep, nq, seed):
     p, db, q = case(name, npep, nq, seed)
