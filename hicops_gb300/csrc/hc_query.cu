@@ -73,18 +73,6 @@ struct SearchArgs
 // phases of k_search timed when SearchArgs::phase is set
 constexpr int kPhases = 6;  // bucket setup | postings stream | score pass 1 | pass 2 | tile clear | rest
 
-__device__ __forceinline__ uint32_t lower_bound_g(const uint32_t *__restrict__ a, uint32_t lo,
-                                                  uint32_t hi, uint32_t v)
-{
-    while (lo < hi)
-    {
-        uint32_t m = lo + ((hi - lo) >> 1);
-        if (__ldg(a + m) < v) lo = m + 1;
-        else hi = m;
-    }
-    return lo;
-}
-
 // The reference's double-precision hyperscore, rounded to float
 // (dslim_query.cpp:695-698). Additions only: no contraction possible.
 __device__ __forceinline__ float exact_h(const QueryConst *__restrict__ qc, uint32_t bc, uint32_t yc,
@@ -259,15 +247,18 @@ __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const f
     return hf > 0.0f;
 }
 
-// Position in a bucket of its first posting whose entry is >= c: a row-table
-// entry when c is a multiple of kRowG, else a search inside that row.
-__device__ __forceinline__ uint32_t row_lb(const uint32_t *__restrict__ col, const uint32_t *__restrict__ qp,
-                                           uint32_t c, uint32_t qsh)
+// Bounds of a bucket's postings for candidates [c0, c1), widened to row-table
+// boundaries (multiples of kRowG entries): the postings of entries outside
+// the range are read but fail the scorecard's index test, so no search is
+// needed. Tile boundaries inside a window are multiples of kRowG already.
+__device__ __forceinline__ uint32_t row_lo(const uint32_t *__restrict__ col, uint32_t c0)
 {
-    const uint32_t k = c / kRowG;
-    const uint32_t lo = __ldg(col + k);
-    if (c == k * kRowG) return lo;
-    return lower_bound_g(qp, lo, __ldg(col + k + 1), c << (qsh + 1));
+    return __ldg(col + c0 / kRowG);
+}
+
+__device__ __forceinline__ uint32_t row_hi(const uint32_t *__restrict__ col, uint32_t c1)
+{
+    return __ldg(col + (c1 + kRowG - 1) / kRowG);
 }
 
 // Warp-level: exclusive chunk offsets of lists [0, np) in place (lo[np] =
@@ -528,26 +519,22 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // j+1's bounds and asks L2 for those postings, which then arrive while
         // the block scores job j.
         Job jb = first_job(T.win, a.nlen, tile);
-        uint32_t pf_lo[kPf], pf_hi[kPf], ps_lo[kPf], ps_hi[kPf];
+        uint32_t pf_hi[kPf], ps_lo[kPf];
+        uint32_t npass = 0;  // postings of entries inside the window (the reference visits exactly these)
         uint32_t cur = 0;
         if (jb.l != kNoJob)
         {
             // the first job's boundaries, directly
             const LenDev d = a.lens[jb.l];
-            uint32_t my_post = 0;
             for (uint32_t pr = tid; pr < np; pr += nthr)
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
-                const uint32_t st = row_lb(col, d.qp, jb.c0, d.qsh);
-                const uint32_t en = row_lb(col, d.qp, jb.c1, d.qsh);
+                const uint32_t st = row_lo(col, jb.c0), en = row_hi(col, jb.c1);
                 linfo[pr] = make_uint2(st, pint[k]);
                 lend[pr] = en;
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                my_post += en - st;
             }
-            my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
-            if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);  // postings visited
             __syncthreads();
             if (wid == 0) chunk_offsets(loff, np, lane, &T.cchunks[0]);
         }
@@ -597,15 +584,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         const uint32_t k = pr / nbin, j = pr - k * nbin;
                         const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                        const uint32_t ke = nj.c1 / kRowG;
-                        pf_lo[m] = __ldg(col + ke);
-                        pf_hi[m] = (nj.c1 == ke * kRowG) ? 0u : __ldg(col + ke + 1);
-                        if (!same)
-                        {
-                            const uint32_t ks = nj.c0 / kRowG;
-                            ps_lo[m] = __ldg(col + ks);
-                            ps_hi[m] = (nj.c0 == ks * kRowG) ? 0u : __ldg(col + ks + 1);
-                        }
+                        pf_hi[m] = row_hi(col, nj.c1);
+                        if (!same) ps_lo[m] = row_lo(col, nj.c0);
                     }
                 }
             }
@@ -661,7 +641,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         for (int e = 0; e < 4; e++)
                         {
                             const uint32_t w = (xs[e] >> d.qsh) - base2;  // 2*(entry - c0) + isY
-                            if (w < lim2) ovf |= atomicAdd(&card[w], add);
+                            if (w < lim2)
+                            {
+                                ovf |= atomicAdd(&card[w], add);
+                                npass++;
+                            }
                         }
                     }
                     else
@@ -671,7 +655,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         for (int e = 0; e < 4; e++)
                         {
                             const uint32_t w = (xs[e] >> d.qsh) - base2;
-                            if (w < lim2) atomicAdd(&card[w], add);
+                            if (w < lim2)
+                            {
+                                atomicAdd(&card[w], add);
+                                npass++;
+                            }
                         }
                     }
                 }
@@ -680,24 +668,16 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             // ---- the next job's list bounds, and its postings into L2 ----
             if (nj.l != kNoJob)
             {
-                uint32_t my_post = 0;
 #pragma unroll
                 for (int m = 0; m < kPf; m++)
                 {
                     const uint32_t pr = tid + m * nthr;
                     if (pr < np)
                     {
-                        const uint32_t st = same ? lend[pr]
-                                                 : (nj.c0 % kRowG == 0u
-                                                        ? ps_lo[m]
-                                                        : lower_bound_g(dn.qp, ps_lo[m], ps_hi[m], nj.c0 << (dn.qsh + 1)));
-                        const uint32_t en = (nj.c1 % kRowG == 0u)
-                                                ? pf_lo[m]
-                                                : lower_bound_g(dn.qp, pf_lo[m], pf_hi[m], nj.c1 << (dn.qsh + 1));
+                        const uint32_t st = same ? lend[pr] : ps_lo[m], en = pf_hi[m];
                         li_n[pr] = make_uint2(st, pint[pr / nbin]);
                         lend[pr] = en;
                         lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                        my_post += en - st;
                         prefetch_l2(dn.qp, st, en);
                     }
                 }
@@ -706,16 +686,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 {
                     const uint32_t k = pr / nbin, j = pr - k * nbin;
                     const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                    const uint32_t st = same ? lend[pr] : row_lb(col, dn.qp, nj.c0, dn.qsh);
-                    const uint32_t en = row_lb(col, dn.qp, nj.c1, dn.qsh);
+                    const uint32_t st = same ? lend[pr] : row_lo(col, nj.c0), en = row_hi(col, nj.c1);
                     li_n[pr] = make_uint2(st, pint[k]);
                     lend[pr] = en;
                     lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                    my_post += en - st;
                     prefetch_l2(dn.qp, st, en);
                 }
-                my_post = __reduce_add_sync(0xFFFFFFFFu, my_post);
-                if (lane == 0 && my_post) atomicAdd(&T.bytes, 4ull * my_post);  // postings visited
             }
             __syncthreads();
             HC_PHASE(1);
@@ -835,6 +811,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
             if (a.phase && nex) atomicAdd(&T.cnt[3], (unsigned long long)nex);
         }
+        // postings visited: those of entries inside the window
+        npass = __reduce_add_sync(0xFFFFFFFFu, npass);
+        if (lane == 0 && npass) atomicAdd(&T.bytes, 4ull * npass);
         // the top hit's shared ions come from the thread that found it
         if (my_best != 0 && my_best == T.best) T.best_shp = my_shp;
         __syncthreads();
