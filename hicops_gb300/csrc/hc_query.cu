@@ -182,11 +182,14 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
 }
 
 // float estimate of the hyperscore; the packed sums are < 2^24, so the
-// integer-to-float conversions stay 32-bit (exact, full-rate)
+// integer-to-float conversions stay 32-bit (exact, full-rate). The two
+// logarithms are one of the product (< 2^48, rounded by 2^-24 relative) with
+// the fast hardware log2: together about 1e-6 off, well inside kApproxErr,
+// which the callers' sign and bin margins are built on.
 __device__ __forceinline__ float approx_h(const float *lgf, uint32_t bc, uint32_t yc, uint64_t ib, uint64_t iy)
 {
     const float fb = __uint2float_rn((uint32_t)ib + 1u), fy = __uint2float_rn((uint32_t)iy + 1u);
-    return ((lgf[bc] + lgf[yc]) + log10f(fb)) + log10f(fy) - 6.0f;
+    return (lgf[bc] + lgf[yc]) + __log2f(fb * fy) * 0.30102999566f - 6.0f;  // one log of the product
 }
 
 __device__ __forceinline__ void decode_packed(uint32_t wb, uint32_t wy, uint32_t &bc, uint32_t &yc, uint32_t &shp,
