@@ -304,7 +304,10 @@ __device__ __forceinline__ void prefetch_l2(const uint32_t *qp, uint32_t st, uin
 }
 
 // One unit of a spectrum's work: the candidates [c0, c1) of length l, at
-// most one scorecard tile (tiles start at multiples of the tile size).
+// most one scorecard tile. A window's first tile ends one tile past the
+// window start rounded down to a row-table boundary (kRowG); every later
+// boundary is a multiple of kRowG, so only a window's two ends widen the
+// postings bounds.
 struct Job
 {
     uint32_t l, c0, c1;
@@ -318,7 +321,7 @@ __device__ __forceinline__ Job job_from(const int2 *win, uint32_t nlen, uint32_t
         if (w.x <= w.y)
         {
             const uint32_t c0 = (uint32_t)w.x;
-            return Job{l, c0, min((uint32_t)w.y + 1, (c0 / tile + 1) * tile)};
+            return Job{l, c0, min((uint32_t)w.y + 1, (c0 / kRowG) * kRowG + tile)};
         }
     }
     return Job{kNoJob, 0u, 0u};
@@ -514,9 +517,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 if (T.win[l].x <= T.win[l].y) atomicAdd(&T.bytes, 4ull * (2 * a.dF + 2) * nv);  // the reference's bA reads
 
         // The spectrum's work is a sequence of jobs (length l, scorecard tile
-        // t). Tiles are aligned to multiples of the tile size, so interior
-        // tile boundaries are row-table entries; only a window's own ends need
-        // a search inside one row. The per-list bounds are double-buffered:
+        // t). Interior tile boundaries are row-table entries; a window's own
+        // ends are widened to the nearest ones (see row_lo / row_hi). The
+        // per-list bounds are double-buffered:
         // while job j streams, the row-table words of job j+1's boundaries are
         // in flight; right after the stream each thread turns them into job
         // j+1's bounds and asks L2 for those postings, which then arrive while
