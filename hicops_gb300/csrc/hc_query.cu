@@ -30,6 +30,7 @@
 #include <cfloat>
 #include <cstring>
 #include <cstdio>
+#include <type_traits>
 
 #include "hc_internal.h"
 
@@ -133,6 +134,7 @@ struct SmemTail
     uint32_t overflow;
     uint32_t spec;
     uint32_t nv;
+    uint32_t noret;            // the stream's atomics need not return the old words (see k_search)
     uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
     uint32_t ndefer;           // undecided candidates queued for the exact evaluation
     uint32_t cchunks[2];       // 16-byte chunks (all lists) of the job in each bound buffer
@@ -509,6 +511,26 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         }
         __syncthreads();
         const uint32_t nv = T.nv < HC_QALEN ? T.nv : HC_QALEN;
+        // The stream's atomics need not return the old words when no word can
+        // reach a count of 128: if every list of the spectrum has a bucket of
+        // its own (valid peaks more than 2*dF bins apart), a candidate's b (y)
+        // count is at most its number of b (y) ions, (L-1)*maxz, below 128 for
+        // every length; with intensities below 2^17 the sums stay below 2^24.
+        if constexpr (!WIDE)
+        {
+            bool close = false;
+            for (uint32_t pr = tid; pr < nv * nv; pr += nthr)
+            {
+                const uint32_t i = pr / nv, j = pr - i * nv;
+                if (i < j)
+                {
+                    const uint32_t x = pmoz[i], y = pmoz[j];
+                    close |= (x > y ? x - y : y - x) <= 2 * a.dF;
+                }
+            }
+            close = __syncthreads_or(close);
+            if (tid == 0) T.noret = (!close && a.lens[a.nlen - 1].half < 128u) ? 1u : 0u;
+        }
         const uint32_t np = nv * nbin;
         my_best = 0;
         my_shp = 0;
@@ -599,6 +621,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             // A warp takes 32*G consecutive chunks; lane j handles chunks
             // q0 + j + 32g. All G loads are issued before any is used.
             uint32_t ovf = 0;  // OR of the words the atomics returned
+            auto stream = [&](auto no_return) {
+            constexpr bool NR = decltype(no_return)::value;
+            (void)NR;
             for (;;)
             {
                 uint32_t q0 = 0;
@@ -649,7 +674,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                             const uint32_t w = (xs[e] >> d.qsh) - base2;  // 2*(entry - c0) + isY
                             if (w < lim2)
                             {
-                                ovf |= atomicAdd(&card[w], add);
+                                if constexpr (NR) atomicAdd(&card[w], add);
+                                else ovf |= atomicAdd(&card[w], add);
                                 npass++;
                             }
                         }
@@ -670,6 +696,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                 }
             }
+            };
+            if (!WIDE && T.noret) stream(std::true_type{});
+            else stream(std::false_type{});
             if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
             // ---- the next job's list bounds, and its postings into L2 ----
             if (nj.l != kNoJob)

@@ -115,6 +115,43 @@ def test_wide_path(dslim, orc):
     ix.close()
 
 
+def test_count_overflow_goes_wide(dslim, orc):
+    """Peaks that share buckets can push a candidate's ion count past 127. Such
+    spectra keep the atomics that return the old scorecard words, see the
+    overflow and are redone wide; spectra with every peak in its own buckets
+    use the other form. Both must agree with the oracle."""
+    p = S.SearchParams(maxz=3, dF=1, dM=500.0)
+    db = S.make_database(2000, 919, p)
+    poly = np.frombuffer(("G" * 39 + "K").encode(), np.uint8).reshape(1, 40)
+    db[40] = np.concatenate([poly, db[40]]) if db[40].shape[0] else poly.copy()
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    e, bA, iA = ix.export(40)
+    k = int(np.nonzero(e["seqid"] == 0)[0][0])      # the poly-G entry
+    speclen = 2 * p.maxz * 39
+    ids = np.nonzero(iA // speclen == k)[0]
+    ions = iA[ids] % speclen
+    bkt = np.searchsorted(bA, ids, side="right") - 1  # bucket of each of its postings
+    bkeys, nb_ions = np.unique(bkt[ions < speclen // 2], return_counts=True)
+    top = bkeys[np.argsort(-nb_ions, kind="stable")[:33]]
+    assert 3 * int(np.sort(nb_ions)[::-1][:33].sum()) >= 128   # the b count the first spectrum reaches
+    thrice = np.repeat(top, 3)                          # every key three times: lists share buckets
+    once = bkeys[np.arange(0, bkeys.size, 3)][:100]     # spread keys: buckets of their own
+    spectra = [thrice, once]
+    idx = np.cumsum([0] + [s.size for s in spectra]).astype(np.uint32)
+    moz = np.concatenate(spectra).astype(np.uint32)
+    inten = np.concatenate([np.linspace(1000, 100000, s.size).astype(np.uint32) for s in spectra])
+    prec = np.full(len(spectra), float(e["mass"][k]), np.float32)
+    q = S.QueryBatch(idx=idx, moz=moz, intensity=inten, precurse=prec,
+                     charges=np.full(len(spectra), 2, np.int32), rtimes=np.zeros(len(spectra), np.float32))
+    res, hist = ix.query(q)
+    assert res["flags"][0] & 0x100, "count overflow not detected"
+    assert not res["flags"][1] & 0x100
+    ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    ix.close()
+
+
 def test_small_tiles(dslim, orc):
     """Many scorecard tiles per length (the smallest tile, windows several tiles wide)."""
     p, db, q = case("mods", 200000, 100, 808)
