@@ -125,6 +125,88 @@ def make_workload(rank: int):
     return p, db, q
 
 
+NEXT_MS2_SPECTRA = int(os.environ.get("HC_NEXT_MS2", "20000"))
+
+
+def next_rows(ix, p, q, res):
+    """The rows either side of the search, measured once after the timed steps:
+    MS2 ingestion (host reader + device peak picking) with the restated reader
+    timed beside it on a small sample, the PSM TSV writer, and the on-disk
+    index (save and restore of the whole index)."""
+    import shutil
+    import tempfile
+    import torch
+    from hicops_gb300 import dslim
+    from hicops_gb300 import synthetic as S
+    out = {}
+    tmp = tempfile.mkdtemp(prefix="hcbench_")
+    try:
+        try:
+            n = min(NEXT_MS2_SPECTRA, q.nspec)
+            path = os.path.join(tmp, "q.ms2")
+            S.write_ms2(path, q, p.scale, n)
+            mb = os.path.getsize(path) / 1e6
+            t = time.perf_counter()
+            rd = dslim.MSQuery(ix).initialize(path)
+            t_parse = time.perf_counter() - t
+            t = time.perf_counter()
+            b, _ = rd.extractbatch(n)
+            t_pick = time.perf_counter() - t
+            rd.DeinitQueryFile()
+            a1 = int(q.idx[n])
+            same = bool(np.array_equal(b.idx, q.idx[:n + 1] - q.idx[0])
+                        and np.array_equal(np.sort(b.intensity), np.sort(q.intensity[:a1]))
+                        and np.array_equal(np.sort(b.moz), np.sort(q.moz[:a1])))
+            ms2 = {"spectra": n, "peaks": a1, "file_mb": mb, "parse_s": t_parse, "pick_s": t_pick,
+                   "spectra_per_s": n / (t_parse + t_pick), "parse_mb_per_s": mb / t_parse,
+                   "pick_spectra_per_s": n / t_pick, "same_peaks_as_written": same}
+            try:
+                from oracle import ms2 as OM  # the restated reader, timed as the CPU baseline of this row
+                ns = min(200, n)
+                small = os.path.join(tmp, "s.ms2")
+                S.write_ms2(small, q, p.scale, ns)
+                t = time.perf_counter()
+                OM.read_ms2(small, p.scale, p.base_int, p.min_int)
+                t_port = time.perf_counter() - t
+                ms2["cpu_baseline"] = {"value": ns / t_port, "unit": "spectra/s", "cores": 1, "kind": "port",
+                                       "sample": f"first {ns} spectra, pure-Python restatement of MSQuery"}
+            except Exception as e:
+                ms2["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+            out["ms2_ingest"] = ms2
+        except Exception as e:
+            out["ms2_ingest"] = {"error": str(e)[:300]}
+        try:
+            path = os.path.join(tmp, "psms.tsv")
+            t = time.perf_counter()
+            ix.write_psms(path, res, q, file_label="bench.ms2")
+            t_tsv = time.perf_counter() - t
+            rows = int((res["reported"] == 1).sum())
+            out["psm_tsv"] = {"rows": rows, "s": t_tsv, "rows_per_s": rows / t_tsv,
+                              "file_mb": os.path.getsize(path) / 1e6}
+        except Exception as e:
+            out["psm_tsv"] = {"error": str(e)[:300]}
+        try:
+            path = os.path.join(tmp, "index.hcd")
+            t = time.perf_counter()
+            ix.save(path)
+            t_save = time.perf_counter() - t
+            gb = os.path.getsize(path) / 1e9
+            ix2 = dslim.Index(p, device=torch.cuda.current_device())
+            t = time.perf_counter()
+            ix2.restore(path)
+            torch.cuda.synchronize()
+            t_rest = time.perf_counter() - t
+            same = all(ix.info(L) == ix2.info(L) for L in range(p.min_len, p.max_len + 1))
+            ix2.close()
+            out["index_file"] = {"gb": gb, "save_s": t_save, "restore_s": t_rest, "save_gb_per_s": gb / t_save,
+                                 "restore_gb_per_s": gb / t_rest, "same_counts": bool(same)}
+        except Exception as e:
+            out["index_file"] = {"error": str(e)[:300]}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def cpu_baseline(p, db, q, threads: int, sample: int):
     """The oracle (CPU restatement of DSLIM_QuerySpectrum) on a bounded sample."""
     from oracle import oracle as O
@@ -522,6 +604,8 @@ def run_gpu(args, rank, world, dist):
             out["cpu_baseline"] = cb
         except Exception as e:  # the baseline is reported, never required
             out["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0 and os.environ.get("HC_NEXT", "1") == "1":
+        out["next_rows"] = next_rows(ix, p, qh, r2)
     if rank == 0:
         print(json.dumps(out), flush=True)
     m.close()

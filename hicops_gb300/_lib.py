@@ -96,6 +96,10 @@ _SIGS = [
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32),
                                  C.POINTER(C.c_uint64)]),
     ("hc_ms2_close", C.c_int, [C.c_void_p]),
+    ("hc_ms2_read", C.c_int, [C.c_char_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint32),
+                              C.POINTER(C.c_uint32)]),
+    ("hc_ms2_raw", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_void_p]),
     ("hc_dslim_query_stream", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),

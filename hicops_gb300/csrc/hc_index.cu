@@ -527,21 +527,41 @@ cudaError_t dalloc(T **p, size_t n)
     return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1));
 }
 
+// Device scratch of one build step, freed when the step returns (also on its
+// error paths).
+struct Scratch
+{
+    std::vector<void *> ptrs;
+    template <class T>
+    cudaError_t alloc(T **p, size_t n)
+    {
+        const cudaError_t e = dalloc(p, n);
+        if (e == cudaSuccess) ptrs.push_back(*p);
+        else *p = nullptr;
+        return e;
+    }
+    ~Scratch()
+    {
+        for (void *p : ptrs) cudaFree(p);
+    }
+};
+
 }  // namespace
 
 // The entries of one length enumerated on the device (k_enum_entries, two
 // passes around a scan of the per-peptide variant counts) into fresh SoA
 // arrays in generation order; sets lh.n.
-static int enumerate_entries(hc_ctx *ctx, LenHost &lh, float **d_m, uint32_t **d_s, uint64_t **d_si,
-                             uint32_t **d_mo, int *launches)
+static int enumerate_entries(hc_ctx *ctx, LenHost &lh, Scratch &out, float **d_m, uint32_t **d_s,
+                             uint64_t **d_si, uint32_t **d_mo, int *launches)
 {
     cudaStream_t st = ctx->stream;
     const uint32_t npep = lh.npep, L = lh.L;
     EnumConst ec;
     make_enum_const(ctx->p, &ec);
+    Scratch tmp;
     uint32_t *cnt = nullptr, *stmp = nullptr;
-    HC_CUDA(ctx, dalloc(&cnt, (size_t)npep + 1));
-    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words((size_t)npep + 1)));
+    HC_CUDA(ctx, tmp.alloc(&cnt, (size_t)npep + 1));
+    HC_CUDA(ctx, tmp.alloc(&stmp, scan_tmp_words((size_t)npep + 1)));
     HC_CUDA(ctx, cudaMemsetAsync(cnt, 0, 4ull * (npep + 1), st));
     const unsigned grid = (npep + 127) / 128;
     if (npep)
@@ -555,17 +575,12 @@ static int enumerate_entries(hc_ctx *ctx, LenHost &lh, float **d_m, uint32_t **d
     HC_CUDA(ctx, cudaMemcpyAsync(&nvar, cnt + npep, 4, cudaMemcpyDeviceToHost, st));
     HC_CUDA(ctx, cudaStreamSynchronize(st));
     const uint64_t n = (uint64_t)npep + nvar;
-    if (n >= (1u << 24))
-    {
-        cudaFree(cnt);
-        cudaFree(stmp);
-        return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^24 entries in one length");
-    }
+    if (n >= (1u << 24)) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^24 entries in one length");
     lh.n = (uint32_t)n;
-    HC_CUDA(ctx, dalloc(d_m, n));
-    HC_CUDA(ctx, dalloc(d_s, n));
-    HC_CUDA(ctx, dalloc(d_si, n));
-    HC_CUDA(ctx, dalloc(d_mo, n));
+    HC_CUDA(ctx, out.alloc(d_m, n));
+    HC_CUDA(ctx, out.alloc(d_s, n));
+    HC_CUDA(ctx, out.alloc(d_si, n));
+    HC_CUDA(ctx, out.alloc(d_mo, n));
     if (npep)
     {
         k_enum_entries<<<grid, 128, 0, st>>>(lh.d_seqs, L, npep, ec, cnt, nullptr, *d_m, *d_s, *d_si, *d_mo);
@@ -573,8 +588,6 @@ static int enumerate_entries(hc_ctx *ctx, LenHost &lh, float **d_m, uint32_t **d
     }
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, cudaStreamSynchronize(st));
-    cudaFree(cnt);
-    cudaFree(stmp);
     return HC_SUCCESS;
 }
 
@@ -583,26 +596,20 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
     cudaStream_t st = ctx->stream;
     int launches = 0;
     // entries in generation order: enumerated here, or uploaded from the host
+    Scratch scr;
     float *d_m0 = nullptr;
     uint32_t *d_s0 = nullptr, *d_mod0 = nullptr;
     uint64_t *d_site0 = nullptr;
     if (!h_entries)
     {
-        const int rc = enumerate_entries(ctx, lh, &d_m0, &d_s0, &d_site0, &d_mod0, &launches);
+        const int rc = enumerate_entries(ctx, lh, scr, &d_m0, &d_s0, &d_site0, &d_mod0, &launches);
         if (rc) return rc;
     }
     const uint32_t n = lh.n, L = lh.L;
     const uint32_t speclen = 2 * ctx->p.maxz * (L - 1);
     const size_t M = (size_t)n * speclen;
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
-    if (M >= 0x80000000ull)
-    {
-        cudaFree(d_m0);
-        cudaFree(d_s0);
-        cudaFree(d_mod0);
-        cudaFree(d_site0);
-        return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^31 ions in one length");
-    }
+    if (M >= 0x80000000ull) return set_error(ctx, HC_ERR_INVLD_SIZE, "more than 2^31 ions in one length");
     if (h_entries && (sort_by_mass && n > 1))
     {
         std::vector<float> hm(n);
@@ -615,10 +622,10 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
             hsite[i] = h_entries[i].sites;
             hmod[i] = h_entries[i].modnum;
         }
-        HC_CUDA(ctx, dalloc(&d_m0, n));
-        HC_CUDA(ctx, dalloc(&d_s0, n));
-        HC_CUDA(ctx, dalloc(&d_mod0, n));
-        HC_CUDA(ctx, dalloc(&d_site0, n));
+        HC_CUDA(ctx, scr.alloc(&d_m0, n));
+        HC_CUDA(ctx, scr.alloc(&d_s0, n));
+        HC_CUDA(ctx, scr.alloc(&d_mod0, n));
+        HC_CUDA(ctx, scr.alloc(&d_site0, n));
         HC_CUDA(ctx, cudaMemcpy(d_m0, hm.data(), 4ull * n, cudaMemcpyHostToDevice));
         HC_CUDA(ctx, cudaMemcpy(d_s0, hs.data(), 4ull * n, cudaMemcpyHostToDevice));
         HC_CUDA(ctx, cudaMemcpy(d_mod0, hmod.data(), 4ull * n, cudaMemcpyHostToDevice));
@@ -634,13 +641,13 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
     const size_t items = M > n ? M : n;
     const size_t ntiles = (items + kRsTile - 1) / kRsTile;
     uint32_t *k0, *k1, *v0, *v1, *hist, *stmp, *d_uninit;
-    HC_CUDA(ctx, dalloc(&k0, items));
-    HC_CUDA(ctx, dalloc(&k1, items));
-    HC_CUDA(ctx, dalloc(&v0, items));
-    HC_CUDA(ctx, dalloc(&v1, items));
-    HC_CUDA(ctx, dalloc(&hist, ntiles * kRadix));
-    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words(ntiles * kRadix)));
-    HC_CUDA(ctx, dalloc(&d_uninit, 1));
+    HC_CUDA(ctx, scr.alloc(&k0, items));
+    HC_CUDA(ctx, scr.alloc(&k1, items));
+    HC_CUDA(ctx, scr.alloc(&v0, items));
+    HC_CUDA(ctx, scr.alloc(&v1, items));
+    HC_CUDA(ctx, scr.alloc(&hist, ntiles * kRadix));
+    HC_CUDA(ctx, scr.alloc(&stmp, scan_tmp_words(ntiles * kRadix)));
+    HC_CUDA(ctx, scr.alloc(&d_uninit, 1));
     HC_CUDA(ctx, cudaMemsetAsync(d_uninit, 0, 4, st));
 
     if (sort_by_mass && n > 1)
@@ -711,20 +718,6 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
     uint32_t h_uninit = 0;
     HC_CUDA(ctx, cudaMemcpyAsync(&h_uninit, d_uninit, 4, cudaMemcpyDeviceToHost, st));
     HC_CUDA(ctx, cudaStreamSynchronize(st));
-    cudaFree(k0);
-    cudaFree(k1);
-    cudaFree(v0);
-    cudaFree(v1);
-    cudaFree(hist);
-    cudaFree(stmp);
-    cudaFree(d_uninit);
-    if (d_m0)
-    {
-        cudaFree(d_m0);
-        cudaFree(d_s0);
-        cudaFree(d_mod0);
-        cudaFree(d_site0);
-    }
     lh.built = true;
     ctx->lens_dirty = true;
     ctx->last_launches = launches + 1;
@@ -751,14 +744,14 @@ int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
     lh.d_qA = lh.d_qp = lh.d_rows = nullptr;
     HC_CUDA(ctx, dalloc(&lh.d_qA, (size_t)nb + 1));
     uint32_t *stmp = nullptr;
-    HC_CUDA(ctx, dalloc(&stmp, scan_tmp_words((size_t)nb + 1)));
+    Scratch scr;
+    HC_CUDA(ctx, scr.alloc(&stmp, scan_tmp_words((size_t)nb + 1)));
     const unsigned bblocks = (unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 16);
     k_pad_counts<<<bblocks, 256, 0, st>>>(lh.d_bA, nb, lh.d_qA);
     HC_CUDA(ctx, scan_exclusive(lh.d_qA, (size_t)nb + 1, stmp, st));
     uint32_t total = 0;
     HC_CUDA(ctx, cudaMemcpyAsync(&total, lh.d_qA + nb, 4, cudaMemcpyDeviceToHost, st));
     HC_CUDA(ctx, cudaStreamSynchronize(st));
-    cudaFree(stmp);
     HC_CUDA(ctx, dalloc(&lh.d_qp, (size_t)total + kIaPad));
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_qp, 0xFF, 4 * ((size_t)total + kIaPad), st));
     if (d_ids && lh.npost)

@@ -13,7 +13,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "hc_internal.h"
@@ -184,37 +186,158 @@ __global__ void k_pick_copy(const uint64_t *__restrict__ off, const uint32_t *__
     }
 }
 
-// strtok_r: next token delimited by runs of any byte in `delim`
-const char *next_tok(const char *&p, const char *delim, size_t &len)
+// One line of the file: [p, e), cut at its first NUL byte as the reference's
+// strtok on c_str() cuts it. The '\n' is not part of it; a '\r' before it is
+// (std::getline keeps it).
+struct Line
 {
-    while (*p && std::strchr(delim, *p)) p++;
-    if (!*p) return nullptr;
-    const char *b = p;
-    while (*p && !std::strchr(delim, *p)) p++;
-    len = (size_t)(p - b);
-    return b;
+    const char *p, *e;
+};
+
+// strtok_r on a line: the next token after runs of ' ' (and '\t' if `tab`)
+bool next_tok(const char *&p, const char *e, bool tab, const char *&tb, const char *&te)
+{
+    while (p < e && (*p == ' ' || (tab && *p == '\t'))) p++;
+    if (p >= e) return false;
+    tb = p;
+    while (p < e && *p != ' ' && !(tab && *p == '\t')) p++;
+    te = p;
+    return true;
 }
 
-std::string tok_or(const char *b, size_t len, const char *dflt) { return b ? std::string(b, len) : std::string(dflt); }
-
-// std::getline: the '\n' is dropped, a '\r' before it stays
-bool read_line(FILE *f, std::string &line)
+// atof / atoi of a token (the token is copied so the conversion cannot read past it)
+double tok_atof(const char *tb, const char *te, double dflt, bool have)
 {
-    line.clear();
-    char buf[4096];
-    bool any = false;
-    while (std::fgets(buf, sizeof(buf), f))
+    if (!have) return dflt;
+    char buf[64];
+    const size_t n = (size_t)(te - tb);
+    if (n < sizeof(buf))
     {
-        any = true;
-        const size_t n = std::strlen(buf);
-        if (n && buf[n - 1] == '\n')
-        {
-            line.append(buf, n - 1);
-            return true;
-        }
-        line.append(buf, n);
+        std::memcpy(buf, tb, n);
+        buf[n] = 0;
+        return std::atof(buf);
     }
-    return any;
+    return std::atof(std::string(tb, n).c_str());
+}
+
+int tok_atoi(const char *tb, const char *te, int dflt, bool have)
+{
+    if (!have) return dflt;
+    char buf[64];
+    const size_t n = (size_t)(te - tb);
+    if (n < sizeof(buf))
+    {
+        std::memcpy(buf, tb, n);
+        buf[n] = 0;
+        return std::atoi(buf);
+    }
+    return std::atoi(std::string(tb, n).c_str());
+}
+
+// The spectra of one stretch of the file. Every stretch but the first starts
+// at an 'S' line; the first holds the file's first 'S' line. A spectrum's
+// charge / precursor (a 'Z' line) and retention time (an 'I RTime' line) are
+// recorded only when one of its lines sets them: the others inherit the
+// previous spectrum's values, which are known once the stretches are joined.
+struct Stretch
+{
+    std::vector<uint8_t> zset, rset;
+    std::vector<uint32_t> z;
+    std::vector<double> prec, rt;
+    std::vector<uint64_t> npk;
+    std::vector<uint32_t> mz, intn;
+    uint64_t peak_lines = 0;
+};
+
+void parse_stretch(const char *b, const char *e, bool first, double scale, Stretch &out)
+{
+    bool started = false;
+    uint8_t zs = 0, rs = 0;
+    uint32_t z = 0;
+    double prec = 0.0, rt = 0.0;
+    uint64_t cur = 0;
+    auto close = [&]() {
+        out.zset.push_back(zs);
+        out.rset.push_back(rs);
+        out.z.push_back(z);
+        out.prec.push_back(prec);
+        out.rt.push_back(rt);
+        out.npk.push_back(cur);
+        zs = rs = 0;
+        cur = 0;
+    };
+    const char *p = b;
+    while (p < e)
+    {
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(e - p)));
+        const char *le = nl ? nl : e;
+        Line ln{p, le};
+        p = nl ? nl + 1 : e;
+        if (ln.p == ln.e) continue;  // empty line
+        const char c = *ln.p;
+        const char *zero = static_cast<const char *>(std::memchr(ln.p, 0, (size_t)(ln.e - ln.p)));
+        const char *ee = zero ? zero : ln.e;
+        const char *q = ln.p, *tb = nullptr, *te = nullptr;
+        if (c == 'H' || c == 'D') continue;
+        if (c == 'Z')
+        {
+            next_tok(q, ee, true, tb, te);
+            bool h = next_tok(q, ee, true, tb, te);
+            z = (uint32_t)tok_atoi(tb, te, 1, h);
+            h = next_tok(q, ee, true, tb, te);
+            prec = tok_atof(tb, te, 0.01, h);
+            zs = 1;
+        }
+        else if (c == 'I')
+        {
+            next_tok(q, ee, true, tb, te);
+            if (next_tok(q, ee, true, tb, te) && te - tb == 5 && std::memcmp(tb, "RTime", 5) == 0)
+            {
+                const bool h = next_tok(q, ee, true, tb, te);
+                rt = tok_atof(tb, te, 0.00, h);
+                rs = 1;
+            }
+        }
+        else if (c == 'S')
+        {
+            if (started) close();
+            started = true;
+        }
+        else
+        {
+            // a peak: tokens split on ' ' only (msquery.cpp:388-404, 478-498); a
+            // missing token reads "0.01" in the file's first spectrum, "0.0" after
+            const double dflt = (first && out.npk.empty()) ? 0.01 : 0.0;
+            bool h = next_tok(q, ee, false, tb, te);
+            const double mzv = tok_atof(tb, te, dflt, h);
+            h = next_tok(q, ee, false, tb, te);
+            const double iv = tok_atof(tb, te, dflt, h);
+            out.mz.push_back((uint32_t)(mzv * scale));
+            out.intn.push_back((uint32_t)(iv * 1000));
+            cur++;
+            out.peak_lines++;
+        }
+    }
+    if (started) close();
+}
+
+// position of the next line start at or after p that begins with 'S' (or e)
+const char *next_s_line(const char *base, const char *p, const char *e)
+{
+    if (p > base && p[-1] != '\n')
+    {
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(e - p)));
+        if (!nl) return e;
+        p = nl + 1;
+    }
+    while (p < e)
+    {
+        if (*p == 'S') return p;
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(e - p)));
+        if (!nl) return e;
+        p = nl + 1;
+    }
+    return e;
 }
 
 void free_scratch(hc_ms2 *m)
@@ -235,90 +358,95 @@ void free_scratch(hc_ms2 *m)
 
 using namespace hc;
 
-extern "C" int hc_ms2_open(hc_ctx *ctx, const char *path, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen)
+extern "C" int hc_ms2_read(const char *path, uint32_t scale_u, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen)
 {
-    if (!ctx || !path || !out) return HC_ERR_INVLD_PTR;
+    if (!path || !out) return HC_ERR_INVLD_PTR;
     *out = nullptr;
     FILE *f = std::fopen(path, "rb");
-    if (!f) return set_error(ctx, HC_ERR_FILE_ERROR, std::string("cannot open ") + path);
-    hc_ms2 *m = new hc_ms2();
-    m->device = ctx->device;
-    const double scale = (double)ctx->p.scale;
-    // MSQuery keeps Z, precursor and retention time in one spectrum_t that is
-    // overwritten line by line, so a spectrum without those lines inherits them
-    uint32_t z = 0;
-    double prec = 0.0, rt = 0.0;
-    bool started = false;
-    uint32_t cur = 0;
-    std::string line;
-    m->off.push_back(0);
-    auto close_spectrum = [&]() {
-        m->prec.push_back(prec);
-        m->z.push_back(z);
-        m->rtime.push_back(rt);
-        m->off.push_back(m->mz.size());
-        if (cur > m->maxslen) m->maxslen = cur;
-        cur = 0;
-    };
-    while (read_line(f, line))
+    if (!f) return HC_ERR_FILE_ERROR;
+    std::vector<char> buf;
+    bool rerr = std::fseek(f, 0, SEEK_END) != 0;
+    const long fsz = rerr ? -1 : std::ftell(f);
+    rerr = rerr || fsz < 0 || std::fseek(f, 0, SEEK_SET) != 0;
+    if (!rerr)
     {
-        if (line.empty() || line[0] == 'H' || line[0] == 'D') continue;
-        const char *p = line.c_str();
-        size_t len = 0;
-        if (line[0] == 'Z')
-        {
-            next_tok(p, " \t", len);
-            const char *a = next_tok(p, " \t", len);
-            z = (uint32_t)std::atoi(tok_or(a, len, "1").c_str());
-            const char *b = next_tok(p, " \t", len);
-            prec = std::atof(tok_or(b, len, "0.01").c_str());
-        }
-        else if (line[0] == 'I')
-        {
-            next_tok(p, " \t", len);
-            const char *a = next_tok(p, " \t", len);
-            if (a && std::string(a, len) == "RTime")
-            {
-                const char *b = next_tok(p, " \t", len);
-                rt = std::atof(tok_or(b, len, "0.00").c_str());
-            }
-        }
-        else if (line[0] == 'S')
-        {
-            if (started) close_spectrum();
-            started = true;
-        }
-        else
-        {
-            // a peak: tokens split on ' ' only (msquery.cpp:388-404, 478-498)
-            const char *dflt = m->prec.empty() ? "0.01" : "0.0";
-            const char *a = next_tok(p, " ", len);
-            const double mzv = std::atof(tok_or(a, len, dflt).c_str());
-            const char *b = next_tok(p, " ", len);
-            const double iv = std::atof(tok_or(b, len, dflt).c_str());
-            m->mz.push_back((uint32_t)(mzv * scale));
-            m->intn.push_back((uint32_t)(iv * 1000));
-            cur++;
-        }
+        buf.resize((size_t)fsz + 1);
+        rerr = std::fread(buf.data(), 1, (size_t)fsz, f) != (size_t)fsz;
+        buf[(size_t)fsz] = 0;
     }
-    const bool rerr = std::ferror(f) != 0;
     std::fclose(f);
-    if (started) close_spectrum();
-    if (rerr)
+    if (rerr) return HC_ERR_FILE_ERROR;
+    const char *base = buf.data(), *end = base + (buf.size() - 1);
+    const double scale = (double)scale_u;
+
+    // stretches: the first runs from the file start through its first 'S'
+    // line; the others start at 'S' lines, about equal in size
+    const char *s0 = next_s_line(base, base, end);
+    const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    const size_t span = (size_t)(end - s0);
+    const unsigned nt = s0 < end ? (unsigned)std::max<size_t>(1, std::min<size_t>(hw, span / (1u << 20) + 1)) : 1u;
+    std::vector<const char *> cut{base};
+    for (unsigned k = 1; k < nt; k++)
     {
-        delete m;
-        return set_error(ctx, HC_ERR_FILE_ERROR, std::string("read failed: ") + path);
+        const char *c = next_s_line(base, s0 + 1 + span * k / nt, end);
+        if (c > cut.back() && c < end) cut.push_back(c);
     }
-    if (m->mz.empty())
+    cut.push_back(end);
+    const size_t ns_ = cut.size() - 1;
+    std::vector<Stretch> parts(ns_);
     {
-        // MSQuery::initialize: no peak line at all (msquery.cpp:143-147)
-        delete m;
-        return set_error(ctx, HC_ERR_INVLD_SIZE, std::string("no peaks in ") + path);
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < ns_; k++)
+            th.emplace_back([&, k]() { parse_stretch(cut[k], cut[k + 1], false, scale, parts[k]); });
+        parse_stretch(cut[0], cut[1], true, scale, parts[0]);
+        for (auto &t : th) t.join();
     }
-    if (m->mz.size() >= 0xFFFFFFFFull || m->off.size() > 0xFFFFFFFFull)
+
+    // join: inherit charge / precursor / retention time in file order (the
+    // reference's spectrum_t starts zeroed, msquery.cpp:27-42)
+    hc_ms2 *m = new hc_ms2();
+    uint64_t peak_lines = 0, nsp = 0, npk = 0;
+    for (const Stretch &st : parts)
+    {
+        peak_lines += st.peak_lines;
+        nsp += st.npk.size();
+        npk += st.mz.size();
+    }
+    m->off.reserve(nsp + 1);
+    m->prec.reserve(nsp);
+    m->z.reserve(nsp);
+    m->rtime.reserve(nsp);
+    m->mz.reserve(npk);
+    m->intn.reserve(npk);
+    m->off.push_back(0);
+    uint32_t cz = 0;
+    double cprec = 0.0, crt = 0.0;
+    for (const Stretch &st : parts)
+    {
+        for (size_t i = 0; i < st.npk.size(); i++)
+        {
+            if (st.zset[i])
+            {
+                cz = st.z[i];
+                cprec = st.prec[i];
+            }
+            if (st.rset[i]) crt = st.rt[i];
+            m->z.push_back(cz);
+            m->prec.push_back(cprec);
+            m->rtime.push_back(crt);
+            m->off.push_back(m->off.back() + st.npk[i]);
+            if (st.npk[i] > m->maxslen) m->maxslen = (uint32_t)std::min<uint64_t>(st.npk[i], 0xFFFFFFFFu);
+        }
+        // peaks of a stretch without an 'S' line (only possible with no 'S' at all) belong to no spectrum
+        const uint64_t used = m->off.back() - m->mz.size();
+        m->mz.insert(m->mz.end(), st.mz.begin(), st.mz.begin() + (ptrdiff_t)used);
+        m->intn.insert(m->intn.end(), st.intn.begin(), st.intn.begin() + (ptrdiff_t)used);
+    }
+    // MSQuery::initialize: no peak line at all is ERR_INVLD_SIZE (msquery.cpp:143-147)
+    if (peak_lines == 0 || m->mz.size() >= 0xFFFFFFFFull || m->off.size() > 0xFFFFFFFFull)
     {
         delete m;
-        return set_error(ctx, HC_ERR_INVLD_SIZE, "MS2 file holds 2^32 peaks or more");
+        return HC_ERR_INVLD_SIZE;
     }
     *out = m;
     if (nspec) *nspec = (uint32_t)m->prec.size();
@@ -326,11 +454,43 @@ extern "C" int hc_ms2_open(hc_ctx *ctx, const char *path, hc_ms2 **out, uint32_t
     return HC_SUCCESS;
 }
 
+extern "C" int hc_ms2_open(hc_ctx *ctx, const char *path, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen)
+{
+    if (!ctx || !path || !out) return HC_ERR_INVLD_PTR;
+    const int rc = hc_ms2_read(path, ctx->p.scale, out, nspec, maxslen);
+    if (rc == HC_ERR_FILE_ERROR) return set_error(ctx, rc, std::string("cannot read ") + path);
+    if (rc == HC_ERR_INVLD_SIZE) return set_error(ctx, rc, std::string("no peaks (or 2^32 or more) in ") + path);
+    return rc;
+}
+
+extern "C" int hc_ms2_raw(const hc_ms2 *m, uint32_t first, uint32_t count, uint64_t *off, uint32_t *mz,
+                          uint32_t *intensity, double *prec, uint32_t *z, double *rtime)
+{
+    if (!m || !off) return HC_ERR_INVLD_PTR;
+    const uint64_t total = m->prec.size();
+    if ((uint64_t)first + count > total) return HC_ERR_INVLD_SIZE;
+    const uint64_t a = m->off[first];
+    for (uint32_t k = 0; k <= count; k++) off[k] = m->off[first + k] - a;
+    const uint64_t n = m->off[first + count] - a;
+    if (mz && n) std::memcpy(mz, m->mz.data() + a, 4 * n);
+    if (intensity && n) std::memcpy(intensity, m->intn.data() + a, 4 * n);
+    for (uint32_t k = 0; k < count; k++)
+    {
+        if (prec) prec[k] = m->prec[first + k];
+        if (z) z[k] = m->z[first + k];
+        if (rtime) rtime[k] = m->rtime[first + k];
+    }
+    return HC_SUCCESS;
+}
+
 extern "C" int hc_ms2_close(hc_ms2 *m)
 {
     if (!m) return HC_SUCCESS;
-    cudaSetDevice(m->device);
-    free_scratch(m);
+    if (m->cap_spec)  // a reader that never extracted made no CUDA call
+    {
+        cudaSetDevice(m->device);
+        free_scratch(m);
+    }
     delete m;
     return HC_SUCCESS;
 }
@@ -355,7 +515,13 @@ extern "C" int hc_ms2_extract(hc_ctx *ctx, hc_ms2 *m, uint32_t first, uint32_t c
     }
     idx[0] = 0;
     if (n == 0) return HC_SUCCESS;
+    if (m->cap_spec && m->device != ctx->device)  // scratch of another device
+    {
+        cudaSetDevice(m->device);
+        free_scratch(m);
+    }
     cudaSetDevice(ctx->device);
+    m->device = ctx->device;
     cudaStream_t st = ctx->stream;
     const uint64_t r0 = m->off[first], r1 = m->off[first + n];
     const size_t nraw = (size_t)(r1 - r0);

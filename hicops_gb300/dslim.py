@@ -255,6 +255,35 @@ class MSQuery:
             pass
 
 
+def read_ms2_raw(path: str, scale: int) -> dict:
+    """An MS2 file's raw spectra as the reference's readspectrum leaves them
+    (before pickpeaks): host only, no device needed (hc_ms2_read + hc_ms2_raw)."""
+    lib = L.load()
+    h = C.c_void_p()
+    n, mx = C.c_uint32(), C.c_uint32()
+    rc = lib.hc_ms2_read(path.encode(), scale, C.byref(h), C.byref(n), C.byref(mx))
+    if rc != 0:
+        raise L.HcError(rc, "hc_ms2_read")
+    try:
+        ns = n.value
+        off = np.zeros(ns + 1, dtype=np.uint64)
+        rc = lib.hc_ms2_raw(h, 0, ns, L.ptr(off), None, None, None, None, None)
+        if rc != 0:
+            raise L.HcError(rc, "hc_ms2_raw")
+        npk = int(off[-1])
+        mz = np.zeros(max(npk, 1), dtype=np.uint32)
+        it = np.zeros_like(mz)
+        prec = np.zeros(ns, dtype=np.float64)
+        z = np.zeros(ns, dtype=np.uint32)
+        rt = np.zeros(ns, dtype=np.float64)
+        rc = lib.hc_ms2_raw(h, 0, ns, L.ptr(off), L.ptr(mz), L.ptr(it), L.ptr(prec), L.ptr(z), L.ptr(rt))
+        if rc != 0:
+            raise L.HcError(rc, "hc_ms2_raw")
+        return dict(off=off, mz=mz[:npk], intensity=it[:npk], prec=prec, z=z, rtime=rt, maxslen=mx.value)
+    finally:
+        lib.hc_ms2_close(h)
+
+
 def DSLIM_Construct(index: Index, L_: int, seqs: np.ndarray) -> int:
     """dslim.h:49 — build one length's index on the device; returns SLM_SUCCESS."""
     index.construct(L_, seqs)

@@ -175,6 +175,30 @@ class QueryBatch:
             self.rtimes.astype(np.float32).tofile(f)
 
 
+def write_ms2(path: str, q: "QueryBatch", scale: int, nspec: int | None = None) -> None:
+    """The first `nspec` spectra of a batch as an MS2 text file (S, I RTime, Z
+    lines, then one "m/z intensity" line per peak) that the reference's reader
+    (MSQuery::readspectrum, msquery.cpp:300-505) turns back into the same
+    integers: each value is written half a unit above itself, so atof * scale
+    (or * 1000) truncates to it; nine digits bring a float32 precursor back."""
+    n = q.nspec if nspec is None else min(int(nspec), q.nspec)
+    idx = np.asarray(q.idx[:n + 1], dtype=np.int64)
+    a, b = int(idx[0]), int(idx[-1])
+    mz = (q.moz[a:b].astype(np.float64) + 0.5) / scale
+    it = (q.intensity[a:b].astype(np.float64) + 0.5) / 1000.0
+    lines = np.char.add(np.char.add(np.char.mod("%.6f", mz), " "), np.char.mod("%.5f", it))
+    with open(path, "w") as f:
+        f.write("H\tCreationDate\tsynthetic\n")
+        for s in range(n):
+            pm = f"{float(q.precurse[s]):.9g}"
+            f.write(f"S\t{s + 1}\t{s + 1}\t{pm}\nI\tRTime\t{float(q.rtimes[s]):.9g}\n"
+                    f"Z\t{int(q.charges[s])}\t{pm}\n")
+            k0, k1 = int(idx[s]) - a, int(idx[s + 1]) - a
+            if k1 > k0:
+                f.write("\n".join(lines[k0:k1].tolist()))
+                f.write("\n")
+
+
 def _pickpeaks(mz_key: np.ndarray, raw_int: np.ndarray, valid: np.ndarray, params: SearchParams):
     """Vectorised restatement of MSQuery::pickpeaks (source/core/msquery.cpp:509-569).
 

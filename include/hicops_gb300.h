@@ -136,7 +136,7 @@ int hc_ctx_get_tuning(const hc_ctx *ctx, hc_tuning *t);
 /* ---- index (DSLIM_Construct, dslim.h:49; LBE_Initialize, lbe.h) ----
  * Builds the SLM index of one peptide length on the device: entries (base
  * peptides in file order, then variable-mod variants, mods.cpp:333-496) are
- * sorted by mass on the device (stable), ion keys are generated, and the
+ * enumerated and sorted by mass on the device (stable), ion keys are generated, and the
  * bucket (bA) and postings (iA) arrays are built by a device radix sort.
  * seqs: npep*L residues (already mass-filtered as LBE_CountPeps does,
  * lbe_internal.cpp:413). order: optional entries in a caller-fixed order
@@ -267,6 +267,18 @@ int hc_write_psms(hc_ctx *ctx, const char *path, const char *file_label, uint32_
  * (the reference's ERR_INVLD_SIZE). */
 typedef struct hc_ms2 hc_ms2;
 int hc_ms2_open(hc_ctx *ctx, const char *path, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen);
+/* The same without a context (host only, no CUDA call): m/z scaled by `scale`.
+ * The file is read once and parsed by all host threads in stretches that
+ * start at 'S' lines; a spectrum without its own 'Z' / 'I RTime' line
+ * inherits the previous one's values, as MSQuery's single spectrum_t does.
+ * Returns the status code only (no context to hold a message). */
+int hc_ms2_read(const char *path, uint32_t scale, hc_ms2 **out, uint32_t *nspec, uint32_t *maxslen);
+/* The raw spectra [first, first+count) as readspectrum leaves them (before
+ * pickpeaks): off[count+1] (relative), mz / intensity (the raw peaks in file
+ * order), prec, z (unsigned, as spectrum_t holds it), rtime; NULL skips an
+ * array. */
+int hc_ms2_raw(const hc_ms2 *m, uint32_t first, uint32_t count, uint64_t *off, uint32_t *mz, uint32_t *intensity,
+               double *prec, uint32_t *z, double *rtime);
 /* Replaces MSQuery::extractbatch (msquery.cpp:239-297) and pickpeaks
  * (msquery.cpp:509-569): spectra [first, first+count) clamped to the file's
  * end (*nout = how many) are peak-picked on the device (quicksort by

@@ -78,16 +78,6 @@ def write_case(path: str, name: str, seed: int = 0, nspec: int = 200, max_peaks:
 
 
 def write_queries(path: str, q, scale: int) -> None:
-    """A picked QueryBatch as MS2 text that reads back to the same integers:
-    each value is written half a unit above itself, so atof * scale (or
-    * 1000) truncates to it."""
-    with open(path, "w") as f:
-        f.write("H\tCreationDate\tsynthetic queries\n")
-        for s in range(q.nspec):
-            a, b = int(q.idx[s]), int(q.idx[s + 1])
-            pm = f"{float(q.precurse[s]):.9g}"  # nine digits bring a float32 back exactly
-            f.write(f"S\t{s + 1}\t{s + 1}\t{pm}\n")
-            f.write(f"I\tRTime\t{float(q.rtimes[s]):.9g}\n")
-            f.write(f"Z\t{int(q.charges[s])}\t{pm}\n")
-            for m, i in zip(q.moz[a:b], q.intensity[a:b]):
-                f.write(f"{(int(m) + 0.5) / scale:.6f} {(int(i) + 0.5) / 1000:.5f}\n")
+    """A picked QueryBatch as MS2 text that reads back to the same integers."""
+    from hicops_gb300 import synthetic as S
+    S.write_ms2(path, q, scale)
