@@ -31,6 +31,7 @@ void free_len(LenHost &lh)
     cudaFree(lh.d_bA);
     cudaFree(lh.d_qA);
     cudaFree(lh.d_qp);
+    cudaFree(lh.d_qion);
     cudaFree(lh.d_rows);
     const uint32_t L = lh.L;
     lh = LenHost();

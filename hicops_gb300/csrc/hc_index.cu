@@ -442,11 +442,11 @@ __global__ void k_bucket_bounds(const uint32_t *__restrict__ skeys, size_t M, ui
 }
 
 // Row table over the query postings: rows[b * stride + k] = first position in
-// bucket b whose entry is >= k * kRowG (a lower bound on k * kRowG << (qsh+1)).
+// bucket b whose entry is >= k * kRowG (a lower bound on k * kRowG << 3).
 // Column 0 is qA[b], column stride-1 is qA[b+1] (padding decodes past every
 // entry, so it never precedes a lower bound).
 __global__ void k_row_table(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp, uint32_t nb,
-                            uint32_t stride, uint32_t n, uint32_t qsh, uint32_t *__restrict__ rows)
+                            uint32_t stride, uint32_t n, uint32_t *__restrict__ rows)
 {
     const uint64_t total = (uint64_t)nb * stride;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -457,7 +457,7 @@ __global__ void k_row_table(const uint32_t *__restrict__ qA, const uint32_t *__r
         if (k == stride - 1) lo = hi;
         else if (k > 0)
         {
-            const uint32_t v = min(k * kRowG, n) << (qsh + 1);
+            const uint32_t v = min(k * kRowG, n) << kQpEntryShift;
             while (lo < hi)
             {
                 const uint32_t m = lo + ((hi - lo) >> 1);
@@ -476,10 +476,10 @@ __global__ void k_pad_counts(const uint32_t *__restrict__ bA, uint32_t nb, uint3
         pc[b] = b < nb ? ((bA[b + 1] - bA[b] + 3u) & ~3u) : 0u;
 }
 
-// ids (entry*speclen + ion, bucket order) -> query postings, one thread per bucket
+// ids (entry*speclen + ion, bucket order) -> query postings and their ions, one thread per bucket
 __global__ void k_qpost(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ ids,
                         const uint32_t *__restrict__ qA, uint32_t nb, uint32_t speclen, uint32_t half,
-                        uint32_t qsh, uint32_t *__restrict__ qp)
+                        uint32_t *__restrict__ qp, uint16_t *__restrict__ qion)
 {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
     {
@@ -487,37 +487,38 @@ __global__ void k_qpost(const uint32_t *__restrict__ bA, const uint32_t *__restr
         for (uint32_t i = s; i < e; i++)
         {
             const uint32_t id = ids[i], entry = id / speclen, ion = id - entry * speclen;
-            qp[q + (i - s)] = (entry << (qsh + 1)) | ((ion >= half ? 1u : 0u) << qsh) | ion;
+            qp[q + (i - s)] = (entry << kQpEntryShift) | ((ion >= half ? 1u : 0u) << 2);
+            qion[q + (i - s)] = (uint16_t)ion;
         }
     }
 }
 
-// counts query-posting words that are neither padding nor an (entry < n, ion < speclen) pair
-__global__ void k_check_qpost(const uint32_t *__restrict__ qp, size_t total, uint32_t n, uint32_t qsh,
-                              uint32_t speclen, uint32_t *__restrict__ bad)
+// counts query-posting words that are neither padding nor an (entry < n, ion < speclen)
+// pair whose b/y bit matches its ion
+__global__ void k_check_qpost(const uint32_t *__restrict__ qp, const uint16_t *__restrict__ qion, size_t total,
+                              uint32_t n, uint32_t speclen, uint32_t half, uint32_t *__restrict__ bad)
 {
     uint32_t b = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
     {
         const uint32_t x = qp[i];
-        if (x != kQpostPad && ((x >> (qsh + 1)) >= n || (x & ((1u << qsh) - 1u)) >= speclen)) b++;
+        if (x == kQpostPad) continue;
+        const uint32_t ion = qion[i];
+        if ((x & 3u) || (x >> kQpEntryShift) >= n || ion >= speclen || ((x >> 2) & 1u) != (ion >= half ? 1u : 0u)) b++;
     }
     if (b) atomicAdd(bad, b);
 }
 
 // query postings -> ids (the reference's iA), one thread per bucket
 __global__ void k_qpost_ids(const uint32_t *__restrict__ bA, const uint32_t *__restrict__ qA,
-                            const uint32_t *__restrict__ qp, uint32_t nb, uint32_t speclen, uint32_t qsh,
-                            uint32_t *__restrict__ ids)
+                            const uint32_t *__restrict__ qp, const uint16_t *__restrict__ qion, uint32_t nb,
+                            uint32_t speclen, uint32_t *__restrict__ ids)
 {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
     {
         const uint32_t s = bA[b], e = bA[b + 1], q = qA[b];
         for (uint32_t i = s; i < e; i++)
-        {
-            const uint32_t x = qp[q + (i - s)];
-            ids[i] = (x >> (qsh + 1)) * speclen + (x & ((1u << qsh) - 1u));
-        }
+            ids[i] = (qp[q + (i - s)] >> kQpEntryShift) * speclen + qion[q + (i - s)];
     }
 }
 
@@ -732,16 +733,15 @@ int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
     cudaStream_t st = ctx->stream;
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
     const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
-    uint32_t qsh = 0;
-    while ((1u << qsh) < speclen) qsh++;
-    // 2*entry+isY must stay below the padding's index and x below 2^32
-    if (lh.n + 2ull > (1ull << (31 - qsh)))
+    // entry << 3 must stay below 2^32 and below the padding word
+    if (lh.n > kQpMaxEntries)
         return set_error(ctx, HC_ERR_INVLD_SIZE, "too many entries of one length for the query postings");
-    lh.qsh = qsh;
     cudaFree(lh.d_qA);
     cudaFree(lh.d_qp);
+    cudaFree(lh.d_qion);
     cudaFree(lh.d_rows);
     lh.d_qA = lh.d_qp = lh.d_rows = nullptr;
+    lh.d_qion = nullptr;
     HC_CUDA(ctx, dalloc(&lh.d_qA, (size_t)nb + 1));
     uint32_t *stmp = nullptr;
     Scratch scr;
@@ -753,14 +753,16 @@ int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
     HC_CUDA(ctx, cudaMemcpyAsync(&total, lh.d_qA + nb, 4, cudaMemcpyDeviceToHost, st));
     HC_CUDA(ctx, cudaStreamSynchronize(st));
     HC_CUDA(ctx, dalloc(&lh.d_qp, (size_t)total + kIaPad));
+    HC_CUDA(ctx, dalloc(&lh.d_qion, (size_t)total + kIaPad));
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_qp, 0xFF, 4 * ((size_t)total + kIaPad), st));
+    HC_CUDA(ctx, cudaMemsetAsync(lh.d_qion, 0, 2 * ((size_t)total + kIaPad), st));
     if (d_ids && lh.npost)
-        k_qpost<<<bblocks, 256, 0, st>>>(lh.d_bA, d_ids, lh.d_qA, nb, speclen, speclen / 2, qsh, lh.d_qp);
+        k_qpost<<<bblocks, 256, 0, st>>>(lh.d_bA, d_ids, lh.d_qA, nb, speclen, speclen / 2, lh.d_qp, lh.d_qion);
     HC_CUDA(ctx, cudaGetLastError());
     return build_rows(ctx, lh);
 }
 
-// The row table of a length from its query postings (qA, qp, qsh, n set).
+// The row table of a length from its query postings (qA, qp, n set).
 int build_rows(hc_ctx *ctx, LenHost &lh)
 {
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
@@ -770,7 +772,7 @@ int build_rows(hc_ctx *ctx, LenHost &lh)
     HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
     const uint64_t rt = (uint64_t)nb * lh.stride;
     const unsigned blocks = (unsigned)std::min<uint64_t>((rt + 255) / 256, (uint64_t)ctx->sm_count * 64);
-    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, lh.qsh, lh.d_rows);
+    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, lh.d_rows);
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HC_SUCCESS;
@@ -783,10 +785,8 @@ int check_query_postings(hc_ctx *ctx, const LenHost &lh, uint64_t qtotal)
 {
     const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
     const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
-    uint32_t q = 0;
-    while ((1u << q) < speclen) q++;
-    if (lh.qsh != q || lh.n + 2ull > (1ull << (31 - q)))
-        return set_error(ctx, HC_ERR_FILE_ERROR, "index file: postings layout does not match the parameters");
+    if (lh.n > kQpMaxEntries)
+        return set_error(ctx, HC_ERR_FILE_ERROR, "index file: too many entries of one length");
     std::vector<uint32_t> qa(nb + 1);
     HC_CUDA(ctx, cudaMemcpy(qa.data(), lh.d_qA, 4ull * (nb + 1), cudaMemcpyDeviceToHost));
     for (uint32_t b = 0; b <= nb; b++)
@@ -800,7 +800,7 @@ int check_query_postings(hc_ctx *ctx, const LenHost &lh, uint64_t qtotal)
     if (e == cudaSuccess && qtotal)
     {
         const unsigned blocks = (unsigned)std::min<uint64_t>((qtotal + 255) / 256, (uint64_t)ctx->sm_count * 32);
-        k_check_qpost<<<blocks, 256, 0, ctx->stream>>>(lh.d_qp, qtotal, lh.n, lh.qsh, speclen, d_bad);
+        k_check_qpost<<<blocks, 256, 0, ctx->stream>>>(lh.d_qp, lh.d_qion, qtotal, lh.n, speclen, speclen / 2, d_bad);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -818,7 +818,7 @@ int export_ids(hc_ctx *ctx, const LenHost &lh, uint32_t *d_ids)
     const uint32_t speclen = 2 * ctx->p.maxz * (lh.L - 1);
     const unsigned bblocks = (unsigned)std::min<uint64_t>((nb + 255) / 256, (uint64_t)ctx->sm_count * 16);
     if (lh.npost)
-        k_qpost_ids<<<bblocks, 256, 0, ctx->stream>>>(lh.d_bA, lh.d_qA, lh.d_qp, nb, speclen, lh.qsh, d_ids);
+        k_qpost_ids<<<bblocks, 256, 0, ctx->stream>>>(lh.d_bA, lh.d_qA, lh.d_qp, lh.d_qion, nb, speclen, d_ids);
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HC_SUCCESS;

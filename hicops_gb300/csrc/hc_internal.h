@@ -22,11 +22,16 @@ constexpr size_t kIaPad = 128;     // postings arrays are padded: the query read
 constexpr uint32_t kRowG = 2048;
 // Query postings: the same postings as the reference's iA (ids entry*speclen
 // + ion, ascending inside each bucket), stored as
-//   (entry << (qsh + 1)) | (isY << qsh) | ion     with 2^qsh >= speclen,
-// so that x >> qsh = 2*entry + isY is a candidate's scorecard word index.
-// Every bucket starts at a multiple of 4 words; the gaps hold kQpostPad,
-// which decodes to an index past every tile.
+//   (entry << 3) | (isY << 2)
+// which is the byte offset of the candidate's scorecard word (two 32-bit
+// words per candidate, b then y) counted from entry 0: a tile starting at
+// entry c0 finds a posting's word at x - (c0 << 3) with no further decoding.
+// The ion of each posting (needed only to give the reference's ids back)
+// sits in a parallel u16 array. Every bucket starts at a multiple of 4 words;
+// the gaps hold kQpostPad, which lies past every tile.
 constexpr uint32_t kQpostPad = 0xFFFFFFFFu;
+constexpr uint32_t kQpEntryShift = 3;
+constexpr uint32_t kQpMaxEntries = (1u << 29) - 2;  // entries of one length the encoding holds
 
 // One peptide length's device-resident index. All arrays are device pointers.
 struct LenDev
@@ -35,7 +40,6 @@ struct LenDev
     uint32_t npep;
     uint32_t magic, msh;           // floor(x / speclen) = umulhi(x, magic) >> msh, x < 2^31
     uint32_t stride;               // row-table entries per bucket: ceil(n / kRowG) + 1
-    uint32_t qsh;                  // ion bits of the query postings
     const float *mass;
     const uint32_t *seqid;
     const uint64_t *sites;
@@ -83,9 +87,9 @@ struct LenHost
     uint32_t *d_bA = nullptr;
     uint32_t *d_qA = nullptr;    // padded bucket starts (max_mass*scale + 1)
     uint32_t *d_qp = nullptr;    // query postings, qA[nb] words (+ kIaPad)
+    uint16_t *d_qion = nullptr;  // ion of each query posting (same positions as d_qp)
     uint32_t *d_rows = nullptr;  // row table (max_mass*scale buckets x stride)
     uint32_t stride = 0;
-    uint32_t qsh = 0;
     bool built = false;
 };
 

@@ -341,6 +341,14 @@ __device__ __forceinline__ Job next_job(const Job &j, const int2 *win, uint32_t 
     return job_from(win, nlen, tile, j.l + 1);
 }
 
+// A job whose bounds are both row-table boundaries inside the length's
+// entries: its lists hold the postings of the job's entries and nothing else
+// (no padding, no neighbours), so their lengths are its visited postings.
+__device__ __forceinline__ bool job_interior(const Job &j, uint32_t n)
+{
+    return (j.c0 % kRowG) == 0 && (j.c1 % kRowG) == 0 && j.c1 < n;
+}
+
 // The last list i in [0, n) with off[i] <= q (off ascending, off[0] = 0):
 // a 32-way search, one shared-memory read per lane per round.
 __device__ __forceinline__ uint32_t find_list(const uint32_t *off, uint32_t n, uint32_t q, int lane)
@@ -554,11 +562,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         {
             // the first job's boundaries, directly
             const LenDev d = a.lens[jb.l];
+            const bool inter = !WIDE && job_interior(jb, d.n);
             for (uint32_t pr = tid; pr < np; pr += nthr)
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
                 const uint32_t st = row_lo(col, jb.c0), en = row_hi(col, jb.c1);
+                if (inter && st < en) npass += en - st;
                 linfo[pr] = make_uint2(st, pint[k]);
                 lend[pr] = en;
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
@@ -619,11 +629,21 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
             // ---- stream the job's postings into the scorecard ----
             // A warp takes 32*G consecutive chunks; lane j handles chunks
-            // q0 + j + 32g. All G loads are issued before any is used.
+            // q0 + j + 32g. All G loads are issued before any is used. A
+            // posting is the byte offset of its scorecard word counted from
+            // entry 0, so one subtraction gives its place in the tile and one
+            // unsigned compare rejects entries outside the tile and padding.
+            // Visited postings are counted per posting only in a window's end
+            // tiles; an interior tile's lists hold exactly the tile's entries,
+            // and their lengths were added when its bounds were set.
             uint32_t ovf = 0;  // OR of the words the atomics returned
-            auto stream = [&](auto no_return) {
+            auto stream = [&](auto no_return, auto count) {
             constexpr bool NR = decltype(no_return)::value;
+            constexpr bool CNT = decltype(count)::value;
             (void)NR;
+            unsigned char *cardb = reinterpret_cast<unsigned char *>(card);
+            const uint32_t base8 = c0 << kQpEntryShift, lim8 = ntile << kQpEntryShift;
+            const uint32_t base2 = 2 * c0, lim2 = 2 * ntile;
             for (;;)
             {
                 uint32_t q0 = 0;
@@ -660,7 +680,6 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         }
                     }
                 }
-                const uint32_t base2 = 2 * c0, lim2 = 2 * ntile;
 #pragma unroll
                 for (int g = 0; g < G; g++)
                 {
@@ -671,12 +690,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 #pragma unroll
                         for (int e = 0; e < 4; e++)
                         {
-                            const uint32_t w = (xs[e] >> d.qsh) - base2;  // 2*(entry - c0) + isY
-                            if (w < lim2)
+                            const uint32_t o = xs[e] - base8;  // byte offset of the word in the tile
+                            if (o < lim8)
                             {
-                                if constexpr (NR) atomicAdd(&card[w], add);
-                                else ovf |= atomicAdd(&card[w], add);
-                                npass++;
+                                uint32_t *wp = reinterpret_cast<uint32_t *>(cardb + o);
+                                if constexpr (NR) atomicAdd(wp, add);
+                                else ovf |= atomicAdd(wp, add);
+                                if constexpr (CNT) npass++;
                             }
                         }
                     }
@@ -686,7 +706,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 #pragma unroll
                         for (int e = 0; e < 4; e++)
                         {
-                            const uint32_t w = (xs[e] >> d.qsh) - base2;
+                            const uint32_t w = (xs[e] >> 2) - base2;  // 2*(entry - c0) + isY
                             if (w < lim2)
                             {
                                 atomicAdd(&card[w], add);
@@ -697,12 +717,26 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 }
             }
             };
-            if (!WIDE && T.noret) stream(std::true_type{});
-            else stream(std::false_type{});
+            if constexpr (WIDE) stream(std::false_type{}, std::true_type{});
+            else
+            {
+                const bool cnt = !job_interior(jb, d.n);
+                if (T.noret)
+                {
+                    if (cnt) stream(std::true_type{}, std::true_type{});
+                    else stream(std::true_type{}, std::false_type{});
+                }
+                else
+                {
+                    if (cnt) stream(std::false_type{}, std::true_type{});
+                    else stream(std::false_type{}, std::false_type{});
+                }
+            }
             if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
             // ---- the next job's list bounds, and its postings into L2 ----
             if (nj.l != kNoJob)
             {
+                const bool inter = !WIDE && job_interior(nj, dn.n);
 #pragma unroll
                 for (int m = 0; m < kPf; m++)
                 {
@@ -710,6 +744,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     if (pr < np)
                     {
                         const uint32_t st = same ? lend[pr] : ps_lo[m], en = pf_hi[m];
+                        if (inter && st < en) npass += en - st;
                         li_n[pr] = make_uint2(st, pint[pr / nbin]);
                         lend[pr] = en;
                         lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
@@ -722,6 +757,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t k = pr / nbin, j = pr - k * nbin;
                     const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
                     const uint32_t st = same ? lend[pr] : row_lo(col, nj.c0), en = row_hi(col, nj.c1);
+                    if (inter && st < en) npass += en - st;
                     li_n[pr] = make_uint2(st, pint[k]);
                     lend[pr] = en;
                     lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
@@ -1301,7 +1337,6 @@ static void fill_lendev(const hc_ctx *ctx, const LenHost &lh, LenDev &d)
     d.bA = lh.d_bA;
     d.qA = lh.d_qA;
     d.qp = lh.d_qp;
-    d.qsh = lh.qsh;
     d.rows = lh.d_rows;
 }
 

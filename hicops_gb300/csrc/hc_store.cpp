@@ -3,10 +3,12 @@
 // hicops.cpp:174-260 calls LBE_Initialize / DSLIM_Construct per length).
 //
 // Layout (little-endian, as the device holds it):
-//   "HCDSLIM1" | u64 params hash | u32 number of lengths
-//   per length: u32 L, npep, n, qsh | u64 npost | u32 nb | u64 qtotal
+//   "HCDSLIM2" | u64 params hash | u32 number of lengths
+//   per length: u32 L, npep, n, entry shift of the postings (3) | u64 npost |
+//               u32 nb | u64 qtotal
 //               seqs u8[npep*L] | mass f32[n] | seqid u32[n] | sites u64[n] |
-//               modnum u32[n] | bA u32[nb+1] | qA u32[nb+1] | qp u32[qtotal]
+//               modnum u32[n] | bA u32[nb+1] | qA u32[nb+1] | qp u32[qtotal] |
+//               ions u16[qtotal]
 // The row tables are rebuilt on load (they are derived from qA/qp).
 #include <algorithm>
 #include <cstdio>
@@ -18,7 +20,7 @@
 
 namespace {
 
-constexpr char kMagic[8] = {'H', 'C', 'D', 'S', 'L', 'I', 'M', '1'};
+constexpr char kMagic[8] = {'H', 'C', 'D', 'S', 'L', 'I', 'M', '2'};
 
 // FNV-1a over every parameter that changes the index's contents
 uint64_t index_hash(const hc_params &p)
@@ -106,13 +108,13 @@ extern "C" int hc_dslim_save(hc_ctx *ctx, const char *path)
         uint32_t qtotal32 = 0;
         if (cudaMemcpy(&qtotal32, lh.d_qA + nb, 4, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
         const uint64_t qtotal = qtotal32;
-        ok = ok && put(f, lh.L) && put(f, lh.npep) && put(f, lh.n) && put(f, lh.qsh) && put(f, lh.npost) &&
+        ok = ok && put(f, lh.L) && put(f, lh.npep) && put(f, lh.n) && put(f, kQpEntryShift) && put(f, lh.npost) &&
              put(f, nb) && put(f, qtotal);
         ok = ok && put_dev(f, lh.d_seqs, (size_t)lh.npep * lh.L, buf);
         ok = ok && put_dev(f, lh.d_mass, 4ull * lh.n, buf) && put_dev(f, lh.d_seqid, 4ull * lh.n, buf);
         ok = ok && put_dev(f, lh.d_sites, 8ull * lh.n, buf) && put_dev(f, lh.d_modnum, 4ull * lh.n, buf);
         ok = ok && put_dev(f, lh.d_bA, 4ull * (nb + 1), buf) && put_dev(f, lh.d_qA, 4ull * (nb + 1), buf);
-        ok = ok && put_dev(f, lh.d_qp, 4ull * qtotal, buf);
+        ok = ok && put_dev(f, lh.d_qp, 4ull * qtotal, buf) && put_dev(f, lh.d_qion, 2ull * qtotal, buf);
     }
     if (!ok || std::fflush(f) != 0) return set_error(ctx, HC_ERR_FILE_ERROR, std::string("write failed: ") + path);
     return HC_SUCCESS;
@@ -137,17 +139,17 @@ extern "C" int hc_dslim_restore(hc_ctx *ctx, const char *path)
     std::vector<char> buf(64u << 20);
     for (uint32_t k = 0; k < nbuilt; k++)
     {
-        uint32_t L = 0, npep = 0, n = 0, qsh = 0, nb = 0;
+        uint32_t L = 0, npep = 0, n = 0, shift = 0, nb = 0;
         uint64_t npost = 0, qtotal = 0;
-        if (!(get(f, L) && get(f, npep) && get(f, n) && get(f, qsh) && get(f, npost) && get(f, nb) && get(f, qtotal)))
+        if (!(get(f, L) && get(f, npep) && get(f, n) && get(f, shift) && get(f, npost) && get(f, nb) && get(f, qtotal)))
             return set_error(ctx, HC_ERR_FILE_ERROR, "truncated index file");
-        if (L < ctx->p.min_len || L > ctx->p.max_len || nb != nb_ctx || qtotal >= 0xFFFFFFFFull)
+        if (L < ctx->p.min_len || L > ctx->p.max_len || nb != nb_ctx || qtotal >= 0xFFFFFFFFull ||
+            shift != kQpEntryShift)
             return set_error(ctx, HC_ERR_FILE_ERROR, "index file does not match this context");
         LenHost &lh = ctx->lens[L - ctx->p.min_len];
         free_len(lh);
         lh.npep = npep;
         lh.n = n;
-        lh.qsh = qsh;
         lh.npost = npost;
         cudaError_t e = cudaMalloc((void **)&lh.d_seqs, (size_t)npep * L + 1);
         if (e == cudaSuccess) e = cudaMalloc((void **)&lh.d_mass, 4ull * n + 4);
@@ -158,6 +160,7 @@ extern "C" int hc_dslim_restore(hc_ctx *ctx, const char *path)
         if (e == cudaSuccess) e = cudaMalloc((void **)&lh.d_qA, 4ull * (nb + 1));
         if (e == cudaSuccess) e = cudaMalloc((void **)&lh.d_qp, 4ull * (qtotal + kIaPad));
         if (e == cudaSuccess) e = cudaMemset(lh.d_qp + qtotal, 0xFF, 4ull * kIaPad);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&lh.d_qion, 2ull * (qtotal + kIaPad));
         if (e != cudaSuccess)
         {
             free_len(lh);
@@ -167,7 +170,7 @@ extern "C" int hc_dslim_restore(hc_ctx *ctx, const char *path)
         ok = ok && get_dev(f, lh.d_mass, 4ull * n, buf) && get_dev(f, lh.d_seqid, 4ull * n, buf);
         ok = ok && get_dev(f, lh.d_sites, 8ull * n, buf) && get_dev(f, lh.d_modnum, 4ull * n, buf);
         ok = ok && get_dev(f, lh.d_bA, 4ull * (nb + 1), buf) && get_dev(f, lh.d_qA, 4ull * (nb + 1), buf);
-        ok = ok && get_dev(f, lh.d_qp, 4ull * qtotal, buf);
+        ok = ok && get_dev(f, lh.d_qp, 4ull * qtotal, buf) && get_dev(f, lh.d_qion, 2ull * qtotal, buf);
         if (!ok)
         {
             free_len(lh);
