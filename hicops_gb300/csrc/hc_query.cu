@@ -159,7 +159,7 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, cmap, defer, linfo, lend, loff, pmoz, pint, wq, tail, total;
+    size_t qual, cmap, defer, linfo, lend, loff, pmoz, pint, wq, sink, tail, total;
     uint32_t maxpairs, loffs;  // linfo / loff entries per buffer (two buffers each)
 };
 
@@ -178,7 +178,8 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     o.pmoz = o.loff + 2 * 4 * (maxpairs + 4);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
-    o.tail = (o.wq + 2ull * kWQ * nwarps + 15) & ~(size_t)15;
+    o.sink = (o.wq + 2ull * kWQ * nwarps + 15) & ~(size_t)15;
+    o.tail = o.sink + 4 * 32;
     o.total = o.tail + sizeof(SmemTail);
     return o;
 }
@@ -250,6 +251,20 @@ __device__ __forceinline__ bool score(const QueryConst *__restrict__ qc, const f
     h = hf;
     bin = hist_bin(hf);
     return hf > 0.0f;
+}
+
+// 32-bit adds to a shared-memory word given by its shared-window address.
+// No memory clobber: the scorecard is read only after a block barrier.
+__device__ __forceinline__ void red_shared_add(uint32_t addr, uint32_t v)
+{
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v));
+}
+
+__device__ __forceinline__ uint32_t atom_shared_add(uint32_t addr, uint32_t v)
+{
+    uint32_t old;
+    asm volatile("atom.shared.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(addr), "r"(v));
+    return old;
 }
 
 // Bounds of a bucket's postings for candidates [c0, c1), widened to row-table
@@ -387,6 +402,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5;
+    // one word per lane that postings outside the tile add to (never read);
+    // the stream addresses the scorecard and the sinks as shared-window offsets
+    const uint32_t card_s = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t sink_s = (uint32_t)__cvta_generic_to_shared(smem + L.sink) + 4u * (uint32_t)lane;
     uint16_t *wq = reinterpret_cast<uint16_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring (tile < 2^16)
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
@@ -690,14 +709,20 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 #pragma unroll
                         for (int e = 0; e < 4; e++)
                         {
-                            const uint32_t o = xs[e] - base8;  // byte offset of the word in the tile
-                            if (o < lim8)
+                            // byte offset of the word in the tile; a posting
+                            // outside the tile (or padding) adds to the lane's
+                            // own sink word instead, so the atomic is not
+                            // behind a branch
+                            const uint32_t o = xs[e] - base8;
+                            const bool in = o < lim8;
+                            const uint32_t wa = in ? card_s + o : sink_s;
+                            if constexpr (NR) red_shared_add(wa, add);
+                            else
                             {
-                                uint32_t *wp = reinterpret_cast<uint32_t *>(cardb + o);
-                                if constexpr (NR) atomicAdd(wp, add);
-                                else ovf |= atomicAdd(wp, add);
-                                if constexpr (CNT) npass++;
+                                const uint32_t old = atom_shared_add(wa, add);
+                                ovf |= in ? old : 0u;
                             }
+                            if constexpr (CNT) npass += in ? 1u : 0u;
                         }
                     }
                     else
