@@ -545,13 +545,14 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // every length; with intensities below 2^17 the sums stay below 2^24.
         if constexpr (!WIDE)
         {
+            // warp w takes peaks i = w, w + nw, ...; its lanes the peaks j > i
             bool close = false;
-            for (uint32_t pr = tid; pr < nv * nv; pr += nthr)
+            for (uint32_t i = (uint32_t)wid; i < nv; i += (uint32_t)(nthr >> 5))
             {
-                const uint32_t i = pr / nv, j = pr - i * nv;
-                if (i < j)
+                const uint32_t x = pmoz[i];
+                for (uint32_t j = i + 1 + (uint32_t)lane; j < nv; j += 32)
                 {
-                    const uint32_t x = pmoz[i], y = pmoz[j];
+                    const uint32_t y = pmoz[j];
                     close |= (x > y ? x - y : y - x) <= 2 * a.dF;
                 }
             }
@@ -816,16 +817,15 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                     __syncwarp();
                 };
-                const uint32_t first = 2 * (tid - (uint32_t)lane), step = 2 * nthr;
-                for (uint32_t base = first; base < ntile; base += step)
-                {
-                    const uint32_t c = base + 2 * (uint32_t)lane;
-                    // words past ntile are zero (the tile is cleared after use)
-                    const uint4 w = c < ntile ? c4[c >> 1] : make_uint4(0u, 0u, 0u, 0u);
+                // a warp covers 128 consecutive candidates per step, as two
+                // halves of 64 (two per lane) whose loads are issued together;
+                // the ring is drained after each half (it never holds more than
+                // 31 + 64 entries)
+                auto push = [&](const uint4 w, uint32_t c) {
                     const uint32_t s0 = (w.x >> 24) + (w.y >> 24), s1 = (w.z >> 24) + (w.w >> 24);
                     const bool q0 = s0 >= a.thr, q1 = s1 >= a.thr;  // thr = max(min_shp, 1)
                     const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, q0), b1 = __ballot_sync(0xFFFFFFFFu, q1);
-                    if ((b0 | b1) == 0) continue;
+                    if ((b0 | b1) == 0) return;
                     const uint32_t lt = (1u << lane) - 1u;
                     const uint32_t r = qhead + qh + (uint32_t)(__popc(b0 & lt) + __popc(b1 & lt));
                     if (q0) wq[r & (kWQ - 1)] = (uint16_t)c;
@@ -837,14 +837,25 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         qhead += 32;
                         qh -= 32;
                     }
+                };
+                const uint32_t first = 4 * (tid - (uint32_t)lane), step = 4 * nthr;
+                for (uint32_t base = first; base < ntile; base += step)
+                {
+                    // words past ntile are zero (the tile is cleared after use)
+                    const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
+                    const uint4 wa = ca < ntile ? c4[ca >> 1] : make_uint4(0u, 0u, 0u, 0u);
+                    const uint4 wb = cb < ntile ? c4[cb >> 1] : make_uint4(0u, 0u, 0u, 0u);
+                    push(wa, ca);
+                    push(wb, cb);
                 }
                 if (qh) pop_score(qh);
                 // the warp's own words, now read: clear them for the next job
                 uint4 *z4 = reinterpret_cast<uint4 *>(card);
                 for (uint32_t base = first; base < ntile; base += step)
                 {
-                    const uint32_t c = base + 2 * (uint32_t)lane;
-                    if (c < ntile) z4[c >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                    const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
+                    if (ca < ntile) z4[ca >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                    if (cb < ntile) z4[cb >> 1] = make_uint4(0u, 0u, 0u, 0u);
                 }
             }
             else
