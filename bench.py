@@ -334,6 +334,112 @@ def run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning):
             "same_psms": mism == 0, "psm_field_mismatches": mism, "batched_tuning": best}
 
 
+def learned_stats(m, d_X, res0, mode: int, thresh: float = 0.1) -> dict:
+    """Learned e-values of one mode for spectra whose expeRT results are res0 (host),
+    with features d_X (device, n x 256): learned share of the reported spectra,
+    fallback rate and |log10 e - log10 e_expeRT| percentiles over the learned ones."""
+    import torch
+    from hicops_gb300._lib import RESULT_DTYPE
+    n = res0.shape[0]
+    d_res = torch.from_numpy(np.frombuffer(res0.tobytes(), dtype=np.uint8).copy()).cuda()
+    learned = torch.empty(n, dtype=torch.float32, device="cuda")
+    nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
+    scr = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+    m.evalues(d_X.data_ptr(), d_res.data_ptr(), n, thresh, learned.data_ptr(), nfb.data_ptr(), scr.data_ptr(),
+              mode=mode)
+    torch.cuda.synchronize()
+    r1 = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=RESULT_DTYPE)
+    ok = (res0["reported"] == 1) & (res0["evalue"] > 0)
+    used = ((r1["flags"] & 0x200) != 0) & ok
+    dl = np.abs(np.log10(r1["evalue"][used]) - np.log10(res0["evalue"][used])) if used.any() else np.zeros(1)
+    return {"mode": mode, "reported": int(ok.sum()), "learned_share": float(used.sum() / max(1, ok.sum())),
+            "fallback_rate": float(1 - used.sum() / max(1, ok.sum())),
+            "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
+            "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
+
+
+def learned_tail_1m(ix, p, db):
+    """Config 3: the learned e-value tail trained on 1,000,000 histograms that the GPU
+    search itself produces. Spectra come from the open-2m generator; each gets a
+    target candidate count drawn log-uniform in [10^2, 10^6] and the precursor window
+    (+-dM Da) that holds that many entries around its precursor mass (bisection on the
+    sorted entry masses of all lengths; achieved percentiles reported). The search runs in sub-batches
+    of 100,000 (expeRT e-values); 80 % of the spectra train the network with the
+    project's own kernels, the other 20 % are held out: there the learned e-values
+    (fallback to expeRT where the refit residual exceeds 0.1) are compared with expeRT's."""
+    import torch
+    from hicops_gb300 import dslim
+    from hicops_gb300 import synthetic as S
+    from hicops_gb300._lib import RESULT_DTYPE, HC_HIST_BINS
+    N = int(os.environ.get("HC_L1M_N", "1000000"))
+    B = min(N, 100000)
+    nb = (N + B - 1) // B
+    ntrain = int(0.8 * N)
+    rng = np.random.default_rng(0xC31)
+    dX = torch.empty(N * 256, dtype=torch.float32, device="cuda")
+    dY = torch.empty(N * 3, dtype=torch.float32, device="cuda")
+    dR = torch.empty(N * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    m = dslim.MLP(ix, seed=0xC32)
+    t_search = t_gen = 0.0
+    counts, wins = [], []
+    allm = np.sort(np.concatenate([ix.entries(L)["mass"].astype(np.float64)
+                                   for L in range(p.min_len, p.max_len + 1)]))
+    cnt = lambda pm, dm: np.searchsorted(allm, pm + dm, "right") - np.searchsorted(allm, pm - dm, "left")
+    try:
+        for b in range(nb):
+            n = min(B, N - b * B)
+            t = time.time()
+            q = S.make_queries(db, n, 0xC31 + 7919 * b, p)
+            target = 10.0 ** rng.uniform(2.0, 6.0, n)
+            pm = q.precurse.astype(np.float64)
+            lo, hi = np.zeros(n), np.full(n, float(p.max_mass))
+            for _ in range(40):
+                mid = 0.5 * (lo + hi)
+                small = cnt(pm, mid) < target
+                lo, hi = np.where(small, mid, lo), np.where(small, hi, mid)
+            q.dM = hi
+            counts.append(cnt(pm, hi))
+            wins.append(hi)
+            t_gen += time.time() - t
+            d = dict(idx=torch.from_numpy(q.idx.astype(np.int32)).cuda(), moz=torch.from_numpy(q.moz.view(np.int32)).cuda(),
+                     inten=torch.from_numpy(q.intensity.view(np.int32)).cuda(), prec=torch.from_numpy(q.precurse).cuda(),
+                     dM=torch.from_numpy(q.dM).cuda(), hist=torch.empty(n * HC_HIST_BINS, dtype=torch.int32, device="cuda"))
+            o = b * B
+            out = dR[o * RESULT_DTYPE.itemsize:(o + n) * RESULT_DTYPE.itemsize]
+            torch.cuda.synchronize()
+            t = time.time()
+            ix.query_device(d["idx"].data_ptr(), d["moz"].data_ptr(), d["inten"].data_ptr(), d["prec"].data_ptr(),
+                            d["dM"].data_ptr(), n, int(q.moz.shape[0]), out.data_ptr(), d["hist"].data_ptr())
+            torch.cuda.synchronize()
+            t_search += time.time() - t
+            m.features(d["hist"].data_ptr(), out.data_ptr(), n, dX[o * 256:].data_ptr())
+            m.targets(out.data_ptr(), n, dY[o * 3:].data_ptr())
+            del d
+        torch.cuda.synchronize()
+        res = np.frombuffer(dR.cpu().numpy().tobytes(), dtype=RESULT_DTYPE).copy()
+        ok = (res["reported"] == 1) & (res["evalue"] > 0)
+        tr = np.nonzero(ok[:ntrain])[0]
+        sel = torch.from_numpy(tr).cuda()
+        Xs, Ys = dX.view(N, 256)[sel].contiguous(), dY.view(N, 3)[sel].contiguous()
+        epochs = int(os.environ.get("HC_L1M_EPOCHS", "20"))
+        t = time.time()
+        loss = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=2048, epochs=epochs, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.time() - t
+        del Xs, Ys
+        Xh = dX[ntrain * 256:]
+        held = {f"mode{k}": learned_stats(m, Xh, res[ntrain:], k) for k in (0, 2)}
+        cc = np.concatenate(counts)
+        return {"histograms": N, "trained_on": int(tr.size), "epochs": epochs, "final_loss": loss,
+                "train_s": t_train, "search_s": t_search, "search_spectra_per_s": N / t_search,
+                "generate_s": t_gen, "windows": "candidate counts log-uniform 1e2-1e6 (window per spectrum)",
+                "window_da_p1_p50_p99": [float(np.percentile(np.concatenate(wins), x)) for x in (1, 50, 99)],
+                "candidates_p1_p50_p99": [float(np.percentile(cc, x)) for x in (1, 50, 99)],
+                "held_out": held}
+    finally:
+        m.close()
+
+
 def run_full(args, rank, world, dist):
     """Config 4: the full pipeline at capacity. 8M peptides + M-ox built on the device;
     1,000,000 spectra of the mixed-window batch streamed from pinned host memory in
@@ -547,6 +653,10 @@ def run_gpu(args, rank, world, dist):
                "fallback_rate": float(1 - used.sum() / max(1, ok.sum())),
                "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
                "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
+    try:  # the agreement-gated mode on the same spectra (not timed)
+        learned["mode2"] = learned_stats(m, dX, res_plain, 2)
+    except Exception as e:
+        learned["mode2"] = {"error": str(e)[:200]}
 
     # ---- uneven batch (mixed precursor windows, 20-150 peaks) on the same index:
     # one plain launch per window class against one batched launch
@@ -606,6 +716,11 @@ def run_gpu(args, rank, world, dist):
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0 and os.environ.get("HC_NEXT", "1") == "1":
         out["next_rows"] = next_rows(ix, p, qh, r2)
+    if rank == 0 and os.environ.get("HC_LEARNED_1M", "1") == "1":
+        try:
+            out["learned_tail_1m"] = learned_tail_1m(ix, p, db)
+        except Exception as e:
+            out["learned_tail_1m"] = {"error": str(e)[:300]}
     if rank == 0:
         print(json.dumps(out), flush=True)
     m.close()

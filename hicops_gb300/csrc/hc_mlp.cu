@@ -197,7 +197,9 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
 // residual there (log10 units) must be within `thresh` (a straight tail over
 // the chosen window), else the spectrum keeps its expeRT e-value.
 // mode 0: network window; mode 1: window from the curve's first bin (the
-// same refit without the network, for comparison).
+// same refit without the network, for comparison); mode 2: mode 0, and the
+// network's predicted line (expeRT's slope and intercept) must also agree
+// with the refitted line at the top hit within `thresh`.
 __global__ void k_learned_evalue(const float *__restrict__ X, const float *__restrict__ out, hc_result *__restrict__ res,
                                  uint32_t n, float thresh, uint32_t min_cpsm, double expect_max, int mode,
                                  float *__restrict__ learned_log10e, uint32_t *__restrict__ nfallback)
@@ -230,7 +232,7 @@ __global__ void k_learned_evalue(const float *__restrict__ X, const float *__res
             if (b) { m2 = q0 - (__ffs(b) - 1); break; }
         }
         last = stt1 + m2;
-        if (mode == 0) first = (int)lrintf(out[s * kOut + 2] / tscale(2));
+        if (mode != 1) first = (int)lrintf(out[s * kOut + 2] / tscale(2));
         else first = stt1;
         first = max(stt1, min(first, last - 1));
         fb = last - first < 1;
@@ -265,10 +267,16 @@ __global__ void k_learned_evalue(const float *__restrict__ X, const float *__res
             se += d * d;
         }
         for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xFFFFFFFFu, se, o);
-        resid = mode == 0 ? sqrtf(se / (float)m) : 0.0f;
+        resid = mode != 1 ? sqrtf(se / (float)m) : 0.0f;
     }
     if (lane != 0) return;
-    if (fb || !(resid <= thresh))
+    // mode 2: the refitted line and the network's predicted line (expeRT's
+    // slope and intercept) at the top hit's hyperscore bin
+    const float agree = mode == 2 && !fb
+                            ? fabsf((slope - out[s * kOut + 0] / tscale(0)) * (float)hyp +
+                                    (icpt - out[s * kOut + 1] / tscale(1)))
+                            : 0.0f;
+    if (fb || !(resid <= thresh) || !(agree <= thresh))
     {
         learned_log10e[s] = NAN;
         atomicAdd(nfallback, 1u);  // keep the expeRT value already in res
@@ -482,7 +490,7 @@ int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, fl
 int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
                         float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream)
 {
-    if (mode != 0 && mode != 1) return HC_ERR_INVLD_PARAM;
+    if (mode < 0 || mode > 2) return HC_ERR_INVLD_PARAM;
     if (!m || (n && (!d_X || !d_res || !d_learned_log10e || !d_nfallback || !d_out_scratch))) return HC_ERR_INVLD_PTR;
     cudaStream_t st = stream ? (cudaStream_t)stream : m->ctx->stream;
     int rc = hc_mlp_forward(m, d_X, n, d_out_scratch, st);

@@ -231,13 +231,16 @@ int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, fl
                    float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
 /* The same with mode 1: the window starts at the curve's first bin (no
  * network) and no residual test is made; the baseline the network is
- * measured against. Mode 0 is hc_mlp_evalues. */
+ * measured against. Mode 0 is hc_mlp_evalues. Mode 2 is mode 0 with a second
+ * test: the network's own predicted tail line (its first two outputs, expeRT's
+ * slope and intercept) must agree with the refitted line at the top hit's
+ * hyperscore within `thresh` (log10 units), else the expeRT value stays. */
 int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
                         float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
 /* ---- on-disk index (no reference counterpart: the reference rebuilds its
  * index on every run, hicops.cpp:174-260) ----
  * hc_dslim_save writes every built length (entries, sequences, bucket offsets
- * and the device postings) to one file with a hash of the index-defining
+ * and the device postings with their ions) to one file with a hash of the index-defining
  * parameters; hc_dslim_restore reads it into a context created with the same
  * parameters (else HC_ERR_INVLD_PARAM) and rebuilds the derived row tables.
  * HC_ERR_FILE_NOT_FOUND / HC_ERR_FILE_ERROR on I/O failures. */

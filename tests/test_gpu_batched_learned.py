@@ -180,6 +180,16 @@ def test_learned_evalues_train_and_fallback():
     m0 = dslim.MLP(ix, seed=12)
     _, _, _, dl_init = run(m0, 0)
     assert good(dlog) > good(dl_base) and good(dlog) > good(dl_init), (good(dlog), good(dl_base), good(dl_init))
+    # mode 2 adds the agreement test: it learns a subset of mode 0's spectra,
+    # keeps expeRT's value elsewhere, and more of what it learns is within 0.05
+    r2, used2, nfb2, dlog2 = run(m, 2)
+    assert not (used2 & ~used).any()
+    assert np.array_equal(r2["evalue"][ok & ~used2], r0["evalue"][ok & ~used2])
+    assert nfb2 == int((ok & ~used2).sum())
+    hu2 = held & used2
+    assert hu2.sum() > 0
+    assert np.mean(dlog2[hu2] <= 0.05) >= np.mean(dlog[hu] <= 0.05), (np.mean(dlog2[hu2] <= 0.05),
+                                                                         np.mean(dlog[hu] <= 0.05))
     m0.close()
     m.close()
     ix.close()
