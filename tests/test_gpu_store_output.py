@@ -64,6 +64,60 @@ def test_restore_rejects_other_parameters_and_bad_files(built, tmp_path):
     ix3.close()
 
 
+def _first_length_layout(blob: bytes):
+    """Offsets of the first length's query postings and ions in an index file
+    ("HCDSLIM2" | hash | count, then per length L, npep, n, shift | npost | nb | qtotal
+    and the arrays seqs, mass, seqid, sites, modnum, bA, qA, qp, ions)."""
+    assert blob[:8] == b"HCDSLIM2"
+    o = 8 + 8 + 4
+    L, npep, n, shift = np.frombuffer(blob, np.uint32, 4, o)
+    npost, = np.frombuffer(blob, np.uint64, 1, o + 16)
+    nb, = np.frombuffer(blob, np.uint32, 1, o + 24)
+    qtotal, = np.frombuffer(blob, np.uint64, 1, o + 28)
+    o += 36 + int(npep) * int(L) + 4 * int(n) * 3 + 8 * int(n) + 8 * (int(nb) + 1)
+    return int(L), int(n), int(shift), int(qtotal), o, o + 4 * int(qtotal)
+
+
+def test_restore_rejects_corrupt_postings(built, tmp_path):
+    """A posting naming an entry past the length's last, an ion past its spectrum,
+    or a b/y bit that does not match its ion makes the file invalid."""
+    from hicops_gb300 import dslim
+    from hicops_gb300._lib import HcError
+    p, db, q, ix, res, hist, path = built
+    blob = bytearray(open(path, "rb").read())
+    L, n, shift, qtotal, o_qp, o_ion = _first_length_layout(bytes(blob))
+    assert shift == 3 and qtotal > 0
+    qp = np.frombuffer(bytes(blob), np.uint32, qtotal, o_qp)
+    k = int(np.nonzero(qp != 0xFFFFFFFF)[0][0])  # a real posting
+    speclen = 2 * p.maxz * (L - 1)
+
+    def rejected(mutate):
+        b = bytearray(blob)
+        mutate(b)
+        bad = tmp_path / "bad.hcd"
+        bad.write_bytes(bytes(b))
+        ix2 = dslim.Index(p)
+        try:
+            with pytest.raises(HcError) as e:
+                ix2.restore(str(bad))
+            return e.value.status
+        finally:
+            ix2.close()
+
+    def entry_past_end(b):
+        b[o_qp + 4 * k:o_qp + 4 * k + 4] = np.uint32((n + 5) << 3).tobytes()
+
+    def ion_past_end(b):
+        b[o_ion + 2 * k:o_ion + 2 * k + 2] = np.uint16(speclen).tobytes()
+
+    def wrong_series(b):
+        x = int(qp[k]) ^ 4  # flip the b/y bit, keep the ion
+        b[o_qp + 4 * k:o_qp + 4 * k + 4] = np.uint32(x).tobytes()
+
+    for f in (entry_past_end, ion_past_end, wrong_series):
+        assert rejected(f) == -3013, f.__name__
+
+
 def test_psm_tsv_columns(built, tmp_path):
     p, db, q, ix, res, hist, path = built
     out = tmp_path / "psms.tsv"
