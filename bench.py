@@ -216,11 +216,27 @@ def cpu_baseline(p, db, q, threads: int, sample: int):
     qs = q.slice(0, min(sample, q.nspec))
     oi.query(qs.slice(0, min(64, qs.nspec)), threads=threads, want_hist=False)  # warm
     t = time.perf_counter()
-    oi.query(qs, threads=threads, want_hist=False)
+    ref, _ = oi.query(qs, threads=threads, want_hist=False)
     dt = time.perf_counter() - t
     return {"value": qs.nspec / dt, "unit": "spectra/s", "cores": threads, "kind": "port",
             "sample": f"first {qs.nspec} spectra of the {q.nspec}-spectrum batch, one pass, "
-                      f"{dt:.1f}s wall"}, oi
+                      f"{dt:.1f}s wall"}, ref
+
+
+def parity_sample(gpu, ref) -> dict:
+    """GPU results (expeRT e-values) against the oracle on the same spectra: integer
+    fields bit-exact, hyperscore within 1e-5 relative, |log10 e| within 0.05."""
+    k = ref.shape[0]
+    g = gpu[:k]
+    exact = {f: int((g[f] != ref[f]).sum()) for f in ("cpsms", "idxoffset", "psid", "sharedions", "reported",
+                                                      "post_bytes")}
+    h = np.abs(g["hyperscore"].astype(np.float64) - ref["hyperscore"]) > 1e-5 * np.abs(ref["hyperscore"]) + 1e-30
+    both = (g["evalue"] > 0) & (ref["evalue"] > 0) & (ref["reported"] == 1)
+    de = np.abs(np.log10(g["evalue"][both]) - np.log10(ref["evalue"][both])) if both.any() else np.zeros(1)
+    return {"spectra": int(k), "mismatches_exact": exact, "hyperscore_over_1e-5": int(h.sum()),
+            "evalues_compared": int(both.sum()), "dlog10e_max": float(de.max()),
+            "evalue_over_0.05": int((de > 0.05).sum()),
+            "identical": bool(not any(exact.values()) and not h.any() and not (de > 0.05).any())}
 
 
 def run_reference(args, rank, world, dist):
@@ -529,8 +545,9 @@ def run_full(args, rank, world, dist):
            "index_build_s": t_build}
     if rank == 0 and not args.no_cpu:
         try:
-            cb, _ = cpu_baseline(p, db, q, os.cpu_count() or 8, int(os.environ.get("HC_CPU_SAMPLE", "1000")))
+            cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8, int(os.environ.get("HC_CPU_SAMPLE", "1000")))
             out["cpu_baseline"] = cb
+            out["parity_vs_oracle"] = parity_sample(r_plain, ref)
         except Exception as e:
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
@@ -710,8 +727,9 @@ def run_gpu(args, rank, world, dist):
     cfg["postings"] = int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1)))
     if rank == 0 and not args.no_cpu:
         try:
-            cb, _ = cpu_baseline(p, db, q, os.cpu_count() or 8, CPU_SAMPLE)
+            cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8, CPU_SAMPLE)
             out["cpu_baseline"] = cb
+            out["parity_vs_oracle"] = parity_sample(res_plain, ref)
         except Exception as e:  # the baseline is reported, never required
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0 and os.environ.get("HC_NEXT", "1") == "1":
