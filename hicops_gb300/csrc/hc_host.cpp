@@ -66,6 +66,7 @@ struct VariantGen
 {
     const hc_params *p;
     int cond_of[26];
+    int nterm = -1;  // mod condition of the N-terminus ('^'), -1 if none
     const uint8_t *seq;
     uint32_t L, seqid;
     hc_entry *out;
@@ -74,10 +75,11 @@ struct VariantGen
     // Depth-first enumeration of MODS_ModList (mods.cpp:333-384): at each
     // position first the branch that modifies it, then the one that does
     // not; an entry is emitted on entering a position right after a new mod.
-    void walk(int *conds, int total, uint64_t sites, uint32_t modnum, int letter, bool novel,
-              int seen)
+    // Positions are virtual: v = 0 is the N-terminus (modifiable only by a
+    // '^' mod, an extension; site bit kNtermBit), v >= 1 is residue v-1.
+    void walk(int *conds, int total, uint64_t sites, uint32_t modnum, int v, bool novel, int seen)
     {
-        if (novel && letter != 0)
+        if (novel)
         {
             if (n < cap && out)
             {
@@ -90,18 +92,18 @@ struct VariantGen
             }
             n++;
         }
-        if (total == 0 || letter >= (int)L)
+        if (total == 0 || v > (int)L)
             return;
-        int c = cond_of[seq[letter] - 'A'];
+        const int c = v == 0 ? nterm : cond_of[seq[v - 1] - 'A'];
+        const int bit = v == 0 ? kNtermBit : v - 1;
         if (c != -1 && conds[c] > 0)
         {
             conds[c] -= 1;
-            walk(conds, total - 1, sites | (1ull << letter),
-                 modnum + (uint32_t)((1u << (4 * seen)) * (uint32_t)(1 + c)), letter + 1, true,
-                 seen + 1);
+            walk(conds, total - 1, sites | (1ull << bit),
+                 modnum + (uint32_t)((1u << (4 * seen)) * (uint32_t)(1 + c)), v + 1, true, seen + 1);
             conds[c] += 1;
         }
-        walk(conds, total, sites, modnum, letter + 1, false, seen);
+        walk(conds, total, sites, modnum, v + 1, false, seen);
     }
 };
 
@@ -116,6 +118,7 @@ void make_enum_const(const hc_params &p, EnumConst *e)
         e->stat[a] = kStatMods[a];
         e->cond_of[a] = -1;
     }
+    e->nterm = -1;
     e->h2o = kH2O;
     const uint32_t nm = p.nmods < HC_MAX_MODS ? p.nmods : HC_MAX_MODS;
     for (uint32_t m = 0; m < nm; m++)
@@ -123,7 +126,8 @@ void make_enum_const(const hc_params &p, EnumConst *e)
         for (int j = 0; j < 4 && p.mod_res[m][j]; j++)
         {
             const int c = p.mod_res[m][j] - 'A';
-            if (c >= 0 && c < 26) e->cond_of[c] = (int8_t)m;
+            if (p.mod_res[m][j] == '^') e->nterm = (int8_t)m;
+            else if (c >= 0 && c < 26) e->cond_of[c] = (int8_t)m;
         }
         e->limit[m] = p.mod_per_pep[m];
         e->modadd[m] = (float)p.mod_mass[m] / (float)p.scale;
@@ -201,7 +205,8 @@ int64_t make_entries(const hc_params &p, uint32_t L, const uint8_t *seqs, uint32
         for (int j = 0; j < 4 && p.mod_res[m][j]; j++)
         {
             int c = p.mod_res[m][j] - 'A';
-            if (c >= 0 && c < 26) g.cond_of[c] = (int)m;
+            if (p.mod_res[m][j] == '^') g.nterm = (int)m;
+            else if (c >= 0 && c < 26) g.cond_of[c] = (int)m;
         }
     for (uint32_t i = 0; i < npep; i++)
     {

@@ -275,11 +275,13 @@ __global__ void k_enum_entries(const uint8_t *__restrict__ seqs, uint32_t L, uin
         const uint64_t at = write ? (uint64_t)npep + voff[i] : 0;
         for (;;)
         {
+            // virtual positions: q = 0 is the N-terminus (a '^' mod, an
+            // extension; site bit kNtermBit), q >= 1 is residue q - 1
             int p = -1;
             if (d < ec.vmods && d < 64)
-                for (uint32_t q = start; q < L; q++)
+                for (uint32_t q = start; q <= L; q++)
                 {
-                    const int c = ec.cond_of[s[q] - 'A'];
+                    const int c = q == 0 ? ec.nterm : ec.cond_of[s[q - 1] - 'A'];
                     if (c >= 0 && cap[c] > 0)
                     {
                         p = (int)q;
@@ -288,11 +290,11 @@ __global__ void k_enum_entries(const uint8_t *__restrict__ seqs, uint32_t L, uin
                 }
             if (p >= 0)
             {
-                const int c = ec.cond_of[s[p] - 'A'];
+                const int c = p == 0 ? ec.nterm : ec.cond_of[s[p - 1] - 'A'];
                 cap[c] -= 1;
                 pos[d] = (uint8_t)p;
                 mn += (1u << ((4u * d) & 31u)) * (uint32_t)(1 + c);  // shift count taken mod 32, as the CPU does
-                st |= 1ull << p;
+                st |= 1ull << (p == 0 ? kNtermBit : p - 1);
                 d++;
                 if (write)
                 {
@@ -311,10 +313,10 @@ __global__ void k_enum_entries(const uint8_t *__restrict__ seqs, uint32_t L, uin
                 if (d == 0) break;
                 d--;
                 const uint32_t q = pos[d];
-                const int c = ec.cond_of[s[q] - 'A'];
+                const int c = q == 0 ? ec.nterm : ec.cond_of[s[q - 1] - 'A'];
                 cap[c] += 1;
                 mn -= (1u << ((4u * d) & 31u)) * (uint32_t)(1 + c);
-                st &= ~(1ull << q);
+                st &= ~(1ull << (q == 0 ? kNtermBit : q - 1));
                 start = q + 1;
             }
         }
@@ -416,6 +418,12 @@ __global__ void k_ion_keys(const IonTables *__restrict__ gt, uint32_t L, uint32_
     uint32_t v = isY ? t.yfm[seq[L - 1] - 'A'][z] : t.bfm[seq[0] - 'A'][z];
     uint32_t madd = 0;
     int cnt = 0;
+    // an N-terminal mod (extension) is the first mod and part of every b ion
+    if (!isY && ((st >> kNtermBit) & 1ull) && seen > 0)
+    {
+        madd = mods[0];
+        cnt = 1;
+    }
     for (uint32_t l = 0; l < Lm1; l++)
     {
         const uint32_t pos = isY ? (L - 1 - l) : l;

@@ -176,12 +176,17 @@ namespace hc {
 // (utils.cpp:290-303), the residue -> mod-condition map and per-condition
 // limits of MODS_ModList (mods.cpp:333-384), and each mod's mass as
 // UTILS_CalculateModMass adds it (float(scaled mass) / float(scale)).
+// Site bit of an N-terminal mod (an extension without a reference
+// counterpart: a mod whose residue code is '^'); residues use bits 0..L-1.
+constexpr int kNtermBit = 63;
+
 struct EnumConst
 {
     float aa[26];
     float stat[26];
     float h2o;
     int8_t cond_of[26];  // mod condition of a residue, -1 if none
+    int8_t nterm;        // mod condition of the N-terminus ('^'), -1 if none
     uint32_t limit[HC_MAX_MODS];
     float modadd[HC_MAX_MODS];
     uint32_t vmods, nmods;

@@ -257,11 +257,20 @@ def make_queries(db: dict[int, np.ndarray], n_spectra: int, seed: int, params: S
         modd = np.zeros(seq.shape, dtype=np.float64)
         pmass = pep_mass_f32(seq)
         if params.mods and params.vmods_per_pep > 0:
-            # random variant: each modifiable residue picked with p=0.5, at most the limit
+            # random variant: each modifiable residue picked with p=0.5, at most the limit;
+            # an N-terminal mod ('^', an extension) first, on the first residue's mass
             first_mod = np.full(rows.size, -1, dtype=np.int64)
             nm = np.zeros(rows.size, dtype=np.int64)
+            for mi, rs in enumerate(mod_res):
+                if rs == "^":
+                    take = (rng.random(rows.size) < 0.5) & (nm < params.vmods_per_pep)
+                    modd[take, 0] += mod_mass[mi]
+                    first_mod = np.where(take & (first_mod < 0), mi, first_mod)
+                    nm += take
             for pos in range(L):
                 for mi, rs in enumerate(mod_res):
+                    if rs == "^":
+                        continue
                     can = np.isin(seq[:, pos], np.frombuffer(rs.encode(), dtype=np.uint8))
                     take = can & (rng.random(rows.size) < 0.5) & (nm < params.vmods_per_pep)
                     modd[take, pos] += mod_mass[mi]
@@ -329,6 +338,10 @@ def make_queries(db: dict[int, np.ndarray], n_spectra: int, seed: int, params: S
                       rtimes=(np.arange(n_spectra) * 0.1).astype(np.float32), dM=dM, source=source)
 
 
+# A variable N-terminal acetylation: residue code '^' marks the peptide's
+# N-terminus (an extension; the reference's mods are residue letters only).
+NTERM_ACETYL = ("^", 42.010565, 1)
+
 # --- the measured workloads (seeds fixed) ---
 
 def workload(name: str):
@@ -345,8 +358,8 @@ def workload(name: str):
     if name == "open-500k":       # open-2m's shape at 1/4 of the database, 2,000 spectra (kernel profiles)
         p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
         return p, 500000, 0xC14, 2000, 0xC15, {}
-    if name == "full-8m":         # 8M peptides + M-ox, 1M spectra of the mixed-window batch, streamed in 50k batches
-        p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+    if name == "full-8m":         # 8M peptides + M-ox + N-term acetyl, 1M spectra of the mixed-window batch, 50k batches
+        p = SearchParams(maxz=3, dF=1, dM=500.0, vmods_per_pep=3, mods=[("M", 15.99, 2), NTERM_ACETYL])
         return p, 8000000, 0xC40, 1000000, 0xC41, dict(
             peaks=(20, 150), window_mix=[(0.5, "ppm", 10.0), (0.3, "da", 50.0), (0.2, "da", 500.0)])
     if name == "mixed-2m":        # open-2m index, 200k spectra, 20-150 peaks, mixed windows

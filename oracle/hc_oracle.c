@@ -12,6 +12,9 @@
 #include <omp.h>
 #endif
 
+/* site bit of an N-terminal mod (extension; residues use bits 0..L-1) */
+#define ORC_NTERM_BIT 63
+
 /* ---------------------------------------------------------------------- */
 /* constants: source/core/utils.cpp:28-101                                  */
 /* ---------------------------------------------------------------------- */
@@ -129,7 +132,8 @@ int orc_gen_spectrum(const uint8_t *seq, uint32_t L, const orc_entry *e, const o
             }
             for (uint32_t z = 0; z < maxz; z++)
             {
-                uint32_t bs = z * (L - 1), counter = 0;
+                /* an N-terminal mod (extension) is the first mod of every b ion */
+                uint32_t bs = z * (L - 1), counter = (uint32_t)((e->sites >> ORC_NTERM_BIT) & 1ull);
                 for (uint32_t l = 0; l < L - 1; l++)
                 {
                     counter += (e->sites >> l) & 1ull;
@@ -172,11 +176,18 @@ int orc_gen_spectrum(const uint8_t *seq, uint32_t L, const orc_entry *e, const o
 /* ---------------------------------------------------------------------- */
 /* entries: LBE_GeneratePeps (lbe_internal.cpp:204-229) and MODS_ModList    */
 /* (mods.cpp:333-384) in depth-first order                                  */
+/*                                                                          */
+/* Extension without a reference counterpart: a mod whose residue code is  */
+/* '^' modifies the peptide's N-terminus. The walk then runs over virtual   */
+/* positions v = 0..L, v = 0 the N-terminus (site bit 63) and v >= 1        */
+/* residue v-1 (site bit v-1); without such a mod, v = 0 is never           */
+/* modifiable and the walk is MODS_ModList's.                               */
 /* ---------------------------------------------------------------------- */
 typedef struct
 {
     const orc_params *p;
     int cond_of[26];
+    int nterm; /* mod index of the N-terminal mod, -1 if none */
     const uint8_t *seq;
     uint32_t L;
     uint32_t seqid;
@@ -185,9 +196,9 @@ typedef struct
 } modgen_t;
 
 static void modlist(modgen_t *g, const int *conds, int total, uint64_t sites, uint32_t modnum,
-                    int letter, int novel, int modsSeen)
+                    int v, int novel, int modsSeen)
 {
-    if (novel && letter != 0)
+    if (novel)
     {
         if (g->n < g->cap)
         {
@@ -200,19 +211,20 @@ static void modlist(modgen_t *g, const int *conds, int total, uint64_t sites, ui
         }
         g->n++;
     }
-    if (total == 0 || letter >= (int)g->L)
+    if (total == 0 || v > (int)g->L)
         return;
-    int c = g->cond_of[g->seq[letter] - 'A'];
+    const int c = v == 0 ? g->nterm : g->cond_of[g->seq[v - 1] - 'A'];
+    const int bit = v == 0 ? ORC_NTERM_BIT : v - 1;
     if (c != -1 && conds[c] > 0)
     {
         int dup[ORC_MAX_MODS];
         memcpy(dup, conds, sizeof(dup));
         dup[c] -= 1;
-        modlist(g, dup, total - 1, sites | (1ull << letter),
-                modnum + (uint32_t)((1u << (4 * modsSeen)) * (uint32_t)(1 + c)), letter + 1, 1,
+        modlist(g, dup, total - 1, sites | (1ull << bit),
+                modnum + (uint32_t)((1u << (4 * modsSeen)) * (uint32_t)(1 + c)), v + 1, 1,
                 modsSeen + 1);
     }
-    modlist(g, conds, total, sites, modnum, letter + 1, 0, modsSeen);
+    modlist(g, conds, total, sites, modnum, v + 1, 0, modsSeen);
 }
 
 int64_t orc_make_entries(const uint8_t *seqs, uint32_t npep, uint32_t L, const orc_params *p,
@@ -226,9 +238,16 @@ int64_t orc_make_entries(const uint8_t *seqs, uint32_t npep, uint32_t L, const o
     g.cap = cap;
     for (int i = 0; i < 26; i++)
         g.cond_of[i] = -1;
+    g.nterm = -1;
     for (uint32_t m = 0; m < p->nmods; m++)
         for (int j = 0; j < 4 && p->mod_res[m][j]; j++)
-            g.cond_of[p->mod_res[m][j] - 'A'] = (int)m;
+        {
+            const int c = p->mod_res[m][j] - 'A';
+            if (p->mod_res[m][j] == '^')
+                g.nterm = (int)m;
+            else if (c >= 0 && c < 26)
+                g.cond_of[c] = (int)m;
+        }
     for (uint32_t i = 0; i < npep; i++)
     {
         if (g.n < cap)

@@ -64,7 +64,8 @@ def _entries_c(p, L_, seqs):
     return out
 
 
-@pytest.mark.parametrize("mods", [[], [("M", 15.99, 2)], [("M", 15.99, 2), ("STY", 79.97, 1)]])
+@pytest.mark.parametrize("mods", [[], [("M", 15.99, 2)], [("M", 15.99, 2), ("STY", 79.97, 1)],
+                                  [("M", 15.99, 2), S.NTERM_ACETYL], [S.NTERM_ACETYL, ("STY", 79.97, 1)]])
 def test_host_entries_match_oracle(mods):
     p = S.SearchParams(maxz=3, vmods_per_pep=2 if mods else 0, mods=mods)
     db = S.make_database(800, 31, p)
@@ -100,3 +101,26 @@ def test_generator_is_seeded():
         assert i1 - i0 <= 100 and np.all(np.diff(it.astype(np.int64)) >= 0)
         if i1 > i0:
             assert it[-1] == p.base_int and it.min() >= p.min_int
+
+
+def test_nterm_mod_variants():
+    """An N-terminal mod (residue code '^', an extension) gives every peptide one
+    variant: site bit 63, the mod's condition in the first modnum nibble, the
+    precursor mass raised by the mod's scaled mass; with a residue mod as well,
+    the N-terminal branch comes first in the walk and its mod is the first nibble."""
+    p = S.SearchParams(maxz=2, vmods_per_pep=1, mods=[S.NTERM_ACETYL])
+    db = S.make_database(300, 41, p)
+    L_ = 12
+    e = _entries_c(p, L_, db[L_])
+    npep = db[L_].shape[0]
+    assert e.shape[0] == 2 * npep
+    v = e[npep:]
+    assert np.all(v["sites"] == np.uint64(1) << np.uint64(63)) and np.all(v["modnum"] == 1)
+    assert np.array_equal(v["seqid"], np.arange(npep))
+    add = np.float32(p.mod_mass_scaled(0)) / np.float32(p.scale)
+    assert np.array_equal(v["mass"], (e["mass"][:npep] + add).astype(np.float32))
+    p2 = S.SearchParams(maxz=2, vmods_per_pep=2, mods=[("M", 15.99, 1), S.NTERM_ACETYL])
+    e2 = O.make_entries(db[L_], L_, p2, sort=False)
+    nt = (e2["sites"] >> np.uint64(63)) & np.uint64(1) == 1
+    assert nt.sum() >= npep
+    assert np.all((e2["modnum"][nt] & 0xF) == 2)  # condition 1 (the N-terminus) is the first mod

@@ -44,7 +44,8 @@ def test_index_bitexact(dslim, orc, name, npep, nq, seed):
 
 @pytest.mark.parametrize("mods,vmods", [([("M", 15.99, 2), ("STY", 79.97, 1)], 3),
                                          ([("M", 15.99, 1), ("NQ", 0.98, 2), ("STY", 79.97, 3)], 4),
-                                         ([("M", 15.99, 3)], 1)])
+                                         ([("M", 15.99, 3)], 1),
+                                         ([("M", 15.99, 2), S.NTERM_ACETYL], 3)])
 def test_device_enumeration_multi_mod(dslim, orc, mods, vmods):
     """Entries enumerated on the device (several mod conditions, per-condition
     limits, a total limit) equal the host enumeration, sorted stably by mass."""
@@ -72,6 +73,29 @@ def test_query_parity(dslim, orc, name, npep, nq, seed):
     ores, ohist = oi.query(q, tie_rule=1)
     st = compare(res, hist, ores, ohist)
     assert st["reported"] > 0
+    ix.close()
+
+
+def test_query_parity_nterm_acetyl(dslim, orc):
+    """The N-terminal acetylation extension (variants, b-ion shift, precursor mass)
+    on the device equals the oracle's restatement of the same rules, and spectra
+    made from acetylated peptides find acetylated entries."""
+    p = S.SearchParams(maxz=3, dF=1, dM=100.0, threads=8, vmods_per_pep=3, mods=[("M", 15.99, 2), S.NTERM_ACETYL])
+    db = S.make_database(3000, 606, p)
+    q = S.make_queries(db, 400, 607, p)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    for L in (p.min_len, 20, p.max_len):
+        e = ix.entries(L)
+        oe = orc.make_entries(db[L], L, p)
+        assert np.array_equal(e.view(np.uint8), oe.view(np.uint8)), f"entries differ at L={L}"
+    res, hist = ix.query(q)
+    oi = orc.OracleIndex(db, p)
+    ores, ohist = oi.query(q, tie_rule=1)
+    compare(res, hist, ores, ohist)
+    sid, mod, site = ix.identity(res)
+    acetyl = (site >> np.uint64(63)) & np.uint64(1) == 1
+    assert acetyl.sum() >= 20, int(acetyl.sum())
     ix.close()
 
 
