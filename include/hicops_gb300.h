@@ -61,7 +61,9 @@ extern "C" {
 
 /* gParams fields on the DSLIM path (slm_dsts.h:359-418). dF is in bins
  * ((uint)(tolerance_Da * scale), hicops.cpp:564); dM in Da; mod_mass is scaled
- * ((uint)(mass * scale), hicops.cpp:661). */
+ * ((uint)(mass * scale), hicops.cpp:661). mod_res holds the residue letters a
+ * mod applies to; the code "^" (no reference counterpart) makes it a mod of
+ * the peptide's N-terminus, recorded as site bit 63 of hc_entry.sites. */
 typedef struct hc_params
 {
     uint32_t min_len, max_len, maxz, topmatches, scale, min_shp, min_cpsm;
