@@ -11,6 +11,11 @@
  * from its own sources by oracle/ref/Makefile and run through
  * oracle/ref/ref_driver.cpp (tests/test_oracle_vs_reference.py, and the golden
  * vectors in tests/golden/ made by tests/golden/make_golden.py).
+ *
+ * One extension has no reference counterpart and so no pinned parity: a mod
+ * whose residue code is "^" modifies the peptide's N-terminus (site bit 63,
+ * the first mod of every b ion); the oracle restates the rules the product
+ * defines for it, and is otherwise the reference's arithmetic unchanged.
  */
 #pragma once
 #include <stdint.h>
