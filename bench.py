@@ -61,8 +61,10 @@ class Clocks:
     """nvidia-smi sampler for the timed region."""
 
     def __init__(self, device: int):
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        import tempfile
+        folder = os.environ.get("HC_CLOCKS_DIR") or tempfile.gettempdir()
+        os.makedirs(folder, exist_ok=True)
+        self.path = os.path.join(folder, f"clocks_bench_{os.getpid()}.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")

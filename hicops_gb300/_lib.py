@@ -21,7 +21,7 @@ STATUS = {0: "success", -3001: "invalid memory", -3002: "invalid parameter", -30
           -3004: "invalid size", -3007: "allocation failed", -3008: "invalid pointer",
           -3010: "invalid modification", -3012: "not enough data", -3006: "file not found",
           -3013: "file error", -3020: "CUDA error",
-          -3021: "device wait timed out", -3022: "no usable CUDA device"}
+          -3021: "work still running at the deadline", -3022: "no usable CUDA device"}
 
 ENTRY_DTYPE = np.dtype([("mass", "<f4"), ("seqid", "<u4"), ("sites", "<u8"),
                         ("modnum", "<u4"), ("pad", "<u4")])
@@ -77,6 +77,7 @@ _SIGS = [
     ("hc_last_error", C.c_char_p, [C.c_void_p]),
     ("hc_ctx_set_tuning", C.c_int, [C.c_void_p, C.POINTER(HcTuning)]),
     ("hc_ctx_get_tuning", C.c_int, [C.c_void_p, C.POINTER(HcTuning)]),
+    ("hc_ctx_wait", C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
     ("hc_dslim_construct", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     ("hc_dslim_load", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                 C.c_void_p, C.c_void_p]),

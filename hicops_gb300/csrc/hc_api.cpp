@@ -1,7 +1,9 @@
 // C ABI of hicops_gb300 (include/hicops_gb300.h): context management, index
 // construction/loading/export, and the host- and device-buffer query calls.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -82,7 +84,7 @@ const char *hc_status_string(int s)
     case HC_ERR_FILE_NOT_FOUND: return "file not found";
     case HC_ERR_FILE_ERROR: return "file error";
     case HC_ERR_CUDA: return "CUDA error";
-    case HC_ERR_TIMEOUT: return "device wait timed out";
+    case HC_ERR_TIMEOUT: return "work still running at the deadline";
     case HC_ERR_NO_DEVICE: return "no usable CUDA device";
     default: return "unknown status";
     }
@@ -198,6 +200,24 @@ int hc_ctx_get_tuning(const hc_ctx *ctx, hc_tuning *t)
     if (!ctx || !t) return HC_ERR_INVLD_PTR;
     *t = ctx->tuning;
     return HC_SUCCESS;
+}
+
+int hc_ctx_wait(hc_ctx *ctx, void *stream, double timeout_s)
+{
+    if (!ctx) return HC_ERR_INVLD_PTR;
+    HC_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;)
+    {
+        const cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) return HC_SUCCESS;
+        if (e != cudaErrorNotReady) return cuda_check(ctx, e, "hc_ctx_wait");
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s >= 0.0 && dt >= timeout_s)
+            return set_error(ctx, HC_ERR_TIMEOUT, "hc_ctx_wait: work still running at the deadline");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
 }
 
 int64_t hc_make_entries(const hc_params *p, uint32_t L, const uint8_t *seqs, uint32_t npep, hc_entry *out,

@@ -438,15 +438,25 @@ __global__ void k_ion_keys(const IonTables *__restrict__ gt, uint32_t L, uint32_
     }
 }
 
+// bA[b] = first position of the sorted keys whose key is >= b, b in [0, nb]
+// (the exclusive scan of the bucket counts, dslim.cpp:97-125): one thread per
+// bucket, a lower bound over the keys. Neighbouring buckets search the same
+// stretch of keys, so the probes share cache lines.
 __global__ void k_bucket_bounds(const uint32_t *__restrict__ skeys, size_t M, uint32_t nb,
                                 uint32_t *__restrict__ bA)
 {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > M) return;
-    // bA[b] = first position whose key >= b, for b in (key[i-1], key[i]]
-    const int64_t prev = (i == 0) ? -1 : (int64_t)skeys[i - 1];
-    const int64_t cur = (i == M) ? (int64_t)nb : (int64_t)skeys[i];
-    for (int64_t b = prev + 1; b <= cur; b++) bA[b] = (uint32_t)i;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= nb;
+         b += (uint64_t)gridDim.x * blockDim.x)
+    {
+        size_t lo = 0, hi = M;
+        while (lo < hi)
+        {
+            const size_t m = lo + ((hi - lo) >> 1);
+            if (__ldg(skeys + m) < (uint32_t)b) lo = m + 1;
+            else hi = m;
+        }
+        bA[b] = (uint32_t)lo;
+    }
 }
 
 // Row table over the query postings: rows[b * stride + k] = first position in
@@ -710,7 +720,8 @@ int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, boo
         HC_CUDA(ctx, radix_sort(k0, k1, v0, v1, M, bits, hist, stmp, st, &which, &launches, true, true));
         uint32_t *skeys = which ? k1 : k0;
         uint32_t *svals = which ? v1 : v0;
-        k_bucket_bounds<<<(unsigned)((M + 1 + 255) / 256), 256, 0, st>>>(skeys, M, nb, lh.d_bA);
+        k_bucket_bounds<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 32), 256, 0,
+                          st>>>(skeys, M, nb, lh.d_bA);
         launches += 1;
         lh.npost = M;
         const int rq = build_query_postings(ctx, lh, svals);

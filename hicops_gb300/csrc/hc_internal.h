@@ -218,6 +218,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
                  hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);
 int sync_lengths(hc_ctx *ctx);
+int preload_query_kernels(hc_ctx *ctx);
 int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                          const float *d_prec, const double *d_dM, uint32_t nspec, hc_result *d_out,
                          uint32_t *d_hist, const ScratchPtrs &s, cudaStream_t st);

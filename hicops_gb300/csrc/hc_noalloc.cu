@@ -5,7 +5,7 @@
 // the request path: the call would fail, or would synchronise the device and
 // stall the other streams of the process. Such callers build the index and
 // create the context beforehand (both allocate) and then search through this
-// entry point, which only copies the small length table and launches kernels.
+// entry point, which only launches kernels.
 //
 // The per-query scratch (precursor windows, overflow list, work counters,
 // longest-first order, tail-fit bins, length table) lives in one file-scope
@@ -14,11 +14,17 @@
 // process exits. All calls on a device share it and it keeps the last call's
 // contents: calls that overlap on the GPU (different streams, or different
 // contexts on the same device) race and must be serialised by the caller.
-// The first call on a device does the set-up: it looks up the array's device
-// address with that device current (cudaGetSymbolAddress, which may load the
-// module), so make it before any stream capture. The work counters, which
-// must start at zero, are cleared by every call on its own stream; every
-// other scratch word is written before it is read.
+//
+// Set-up. The first call in a CUDA context (normally a device's primary
+// context) looks up the array's device address in that context
+// (cudaGetSymbolAddress) and loads every kernel the search can launch, so
+// that no later call loads code (with lazy module loading, the default, a
+// kernel's first launch would load it and allocate device memory for it).
+// Make that first call before any stream capture. The address and the
+// loaded kernels belong to the context, so the cache is keyed by the
+// context current at the call, not by the device ordinal. The work
+// counters, which must start at zero, are cleared by every call on its own
+// stream; every other scratch word is written before it is read.
 #include <cstring>
 #include <mutex>
 
@@ -39,11 +45,63 @@ constexpr size_t kLensOff = kFitOff + al(4ull * kNoAllocMaxSpectra);
 constexpr size_t kScratchBytes = kLensOff + al(sizeof(LenDev) * HC_MAX_LENGTHS);  // about 8.5 MB
 
 // The scratch itself. Host code must not use the symbol as an address: its
-// device address comes from cudaGetSymbolAddress, once per device.
+// device address comes from cudaGetSymbolAddress, once per CUDA context.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
-unsigned char *g_addr[256] = {};  // device address of g_noalloc_scratch, per device ordinal
+
+// One set-up per CUDA context: its handle and the array's address in it.
+struct CtxSlot
+{
+    void *cu_ctx;
+    unsigned char *addr;
+};
+constexpr int kMaxCtx = 64;
+CtxSlot g_slot[kMaxCtx] = {};
+int g_nslot = 0;
+
+// cuCtxGetCurrent from the driver, looked up once through the runtime (the
+// library does not link the driver library itself)
+using CtxGetCurrent = int (*)(void **);
+CtxGetCurrent ctx_get_current()
+{
+    static CtxGetCurrent fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    return fn;
+}
+
+// The array's address in the current context, setting the context up on
+// its first call. Caller holds g_mu and has made the context's device current.
+int scratch_address(hc_ctx *ctx, unsigned char **out)
+{
+    // a runtime call first, so that the device's primary context is current
+    // when the caller has not made another one current
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    void *cur = nullptr;
+    const CtxGetCurrent get = ctx_get_current();
+    if (!get || get(&cur) != 0 || !cur)
+        return set_error(ctx, HC_ERR_CUDA, "hc_dslim_query_noalloc: no current CUDA context");
+    for (int i = 0; i < g_nslot; i++)
+        if (g_slot[i].cu_ctx == cur)
+        {
+            *out = g_slot[i].addr;
+            return HC_SUCCESS;
+        }
+    if (g_nslot == kMaxCtx) return set_error(ctx, HC_ERR_INVLD_SIZE, "hc_dslim_query_noalloc: too many CUDA contexts");
+    const int rc = preload_query_kernels(ctx);
+    if (rc) return rc;
+    g_slot[g_nslot++] = CtxSlot{cur, static_cast<unsigned char *>(p)};
+    *out = static_cast<unsigned char *>(p);
+    return HC_SUCCESS;
+}
 
 }  // namespace
 }  // namespace hc
@@ -59,23 +117,16 @@ extern "C" int hc_dslim_query_noalloc(hc_ctx *ctx, const uint32_t *d_idx, const 
     if (!ctx) return HC_ERR_INVLD_PTR;
     if (nspec > kNoAllocMaxSpectra)
         return set_error(ctx, HC_ERR_INVLD_SIZE, "hc_dslim_query_noalloc: more than 16384 spectra in one call");
-    if (ctx->lens.size() > HC_MAX_LENGTHS || ctx->device < 0 || ctx->device >= 256)
+    if (ctx->lens.size() > HC_MAX_LENGTHS)
         return set_error(ctx, HC_ERR_INVLD_SIZE, "hc_dslim_query_noalloc: too many peptide lengths");
     if (nspec && (!d_idx || !d_moz || !d_intensity || !d_precurse || !d_out || !d_hist))
         return set_error(ctx, HC_ERR_INVLD_PTR, "null device buffer");
     HC_CUDA(ctx, cudaSetDevice(ctx->device));
     unsigned char *base = nullptr;
     {
-        // set-up on the first call on this device, with the device current
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[ctx->device])
-        {
-            void *p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) return cuda_check(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-            g_addr[ctx->device] = static_cast<unsigned char *>(p);
-        }
-        base = g_addr[ctx->device];
+        const int rc = scratch_address(ctx, &base);
+        if (rc) return rc;
     }
     ScratchPtrs s;
     s.win = reinterpret_cast<int2 *>(base + kWinOff);

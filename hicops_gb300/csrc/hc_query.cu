@@ -1490,21 +1490,69 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     return HC_SUCCESS;
 }
 
+namespace {
+
+// The length table of one query, passed by value as a kernel parameter
+// (7 KB, inside the 32 KB parameter space), so that writing it to device
+// scratch needs neither a host copy nor a host buffer that must outlive the call.
+struct LenTable
+{
+    LenDev l[HC_MAX_LENGTHS];
+};
+
+__global__ void k_put_lens(const LenTable t, uint32_t nlen, LenDev *__restrict__ dst)
+{
+    if (threadIdx.x < nlen) dst[threadIdx.x] = t.l[threadIdx.x];
+}
+
+template <class F>
+cudaError_t load_one(F *f)
+{
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, f);
+}
+
+}  // namespace
+
+// Loads every kernel launch_query_scratch can launch into the current
+// context. With lazy module loading (the default) a kernel's code is loaded,
+// and device memory allocated for it, at its first launch; asking for its
+// attributes loads it now instead.
+int preload_query_kernels(hc_ctx *ctx)
+{
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(load_one(k_put_lens));
+    chk(load_one(k_windows));
+    chk(load_one(k_cost));
+    chk(load_one(k_order));
+    chk(load_one(k_tailfit));
+    chk(load_one(k_search<false, 1>));
+    chk(load_one(k_search<false, 2>));
+    chk(load_one(k_search<false, 4>));
+    chk(load_one(k_search<false, 8>));
+    chk(load_one(k_search<true, 2>));
+    HC_CUDA(ctx, e);
+    return HC_SUCCESS;
+}
+
 // The query pipeline of query_device with every scratch buffer supplied by
 // the caller (used by the allocation-free entry point): the length table is
-// copied into s.lens, nothing is allocated and the host does not wait.
+// written into s.lens by a kernel that takes it as a parameter, nothing is
+// allocated and the host does not wait.
 int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                          const float *d_prec, const double *d_dM, uint32_t nspec, hc_result *d_out,
                          uint32_t *d_hist, const ScratchPtrs &s, cudaStream_t st)
 {
     const uint32_t nlen = (uint32_t)ctx->lens.size();
-    LenDev h[HC_MAX_LENGTHS];
+    LenTable t;
+    std::memset(&t, 0, sizeof(t));
     for (uint32_t i = 0; i < nlen; i++)
     {
-        fill_lendev(ctx, ctx->lens[i], h[i]);
+        fill_lendev(ctx, ctx->lens[i], t.l[i]);
     }
-    // pageable source: the copy is staged before the call returns
-    HC_CUDA(ctx, cudaMemcpyAsync(s.lens, h, sizeof(LenDev) * nlen, cudaMemcpyHostToDevice, st));
+    k_put_lens<<<1, HC_MAX_LENGTHS, 0, st>>>(t, nlen, s.lens);
+    HC_CUDA(ctx, cudaGetLastError());
     ctx->last_launches = 0;
     if (nspec == 0) return HC_SUCCESS;
     uint32_t *nwide = s.work + 2;
@@ -1561,7 +1609,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
                                                                             ctx->p.expect_max, s.fitstart);
     HC_CUDA(ctx, cudaGetLastError());
-    ctx->last_launches = launches;
+    ctx->last_launches = launches + 1;
     return HC_SUCCESS;
 }
 

@@ -43,7 +43,7 @@ extern "C" {
 #define HC_ERR_FILE_ERROR (-3013)
 /* codes without a reference counterpart */
 #define HC_ERR_CUDA (-3020)      /* a CUDA runtime call failed; see hc_last_error */
-#define HC_ERR_TIMEOUT (-3021)   /* a bounded device wait ran out */
+#define HC_ERR_TIMEOUT (-3021)   /* hc_ctx_wait: the work was still running at the deadline */
 #define HC_ERR_NO_DEVICE (-3022) /* no CUDA device, or not an sm_103 part */
 
 #define HC_HIST_BINS 1002 /* 2 + MAX_HYPERSCORE*10 (dslim.cpp:419) */
@@ -134,6 +134,14 @@ int hc_ctx_destroy(hc_ctx *ctx);
 const char *hc_last_error(const hc_ctx *ctx);
 int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t);
 int hc_ctx_get_tuning(const hc_ctx *ctx, hc_tuning *t);
+/* Waits at most timeout_s seconds (< 0: no limit) for the device work
+ * enqueued on `stream` (cudaStream_t; NULL = the context stream), e.g. by
+ * hc_dslim_query_device. HC_SUCCESS: it has finished; HC_ERR_TIMEOUT: it was
+ * still running at the deadline (nothing is cancelled: wait again later);
+ * HC_ERR_CUDA: it failed. Replaces the reference's unbounded wait for a
+ * batch (the manager thread joining DSLIM_QuerySpectrum, dslim_query.cpp:361)
+ * for callers that serve requests with deadlines. */
+int hc_ctx_wait(hc_ctx *ctx, void *stream, double timeout_s);
 
 /* ---- index (DSLIM_Construct, dslim.h:49; LBE_Initialize, lbe.h) ----
  * Builds the SLM index of one peptide length on the device: entries (base
@@ -182,9 +190,11 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
  * same arguments and results, but its scratch is a fixed file-scope device
  * array, so it never allocates, for callers that may not allocate device
  * memory while they search. At most 16384 spectra per call (larger batches
- * return HC_ERR_INVLD_SIZE). The first call on a device sets up the scratch
- * address and should come before any stream capture. All calls on one device
- * share the scratch: calls that overlap on the GPU race. */
+ * return HC_ERR_INVLD_SIZE). The first call in a CUDA context (normally the
+ * device's primary context) does the set-up: it looks up the scratch address
+ * and loads every kernel the search can launch, so that later calls load no
+ * code; make it before any stream capture. All calls on one device share the
+ * scratch: calls that overlap on the GPU race. */
 int hc_dslim_query_noalloc(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz,
                            const uint32_t *d_intensity, const float *d_precurse,
                            const double *d_dM, uint32_t nspec, uint32_t npeaks,

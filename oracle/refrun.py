@@ -31,8 +31,15 @@ def available() -> bool:
     return os.path.exists(DRIVER)
 
 
-def build(ref_root: str = "/root/reference") -> bool:
+def reference_dir() -> str:
+    """Where the reference sources are mounted: $HC_REFERENCE_DIR, else the
+    read-only mount of the build container."""
+    return os.environ.get("HC_REFERENCE_DIR") or "/root/reference"
+
+
+def build(ref_root: str | None = None) -> bool:
     """Compile the reference into oracle/_ref when its sources are present."""
+    ref_root = ref_root or reference_dir()
     if not os.path.isdir(ref_root):
         return False
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}",

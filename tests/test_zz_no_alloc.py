@@ -1,9 +1,15 @@
 """GPU test of the allocation-free query entry point (hc_dslim_query_noalloc),
 called through the C ABI and compared with hc_dslim_query_device on the same
 device buffers. Collected last so that it also runs after every other test
-has used the library in this process.
+has used the library in this process; one case runs in a fresh process,
+where the entry point is the first search, and checks that after its set-up
+call no call changes the device's free memory.
 """
 import ctypes as C
+import json
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -98,3 +104,63 @@ def test_noalloc_rejects_oversized_batch():
     assert rc == 0, ix.lib.hc_last_error(ix.ctx)
     torch.cuda.synchronize()
     ix.close()
+
+
+# Child process: the index is built (that allocates), then the first search
+# of the process is the allocation-free one (its set-up call). Free device
+# memory is read after it and after three more calls with other launch shapes
+# (persistent in batch order, longest-first with another lists-in-flight
+# count, one CTA per spectrum); only then does hc_dslim_query_device run, for
+# the comparison.
+_CHILD = r"""
+import ctypes as C, json, sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from hicops_gb300 import dslim, synthetic as S
+from tests.test_zz_no_alloc import _dev, _out, _args, _results
+from tests._util import compare
+p = S.SearchParams(maxz=3, dF=1, dM=500.0, threads=8, vmods_per_pep=2, mods=[("M", 15.99, 2)])
+db = S.make_database(3000, 1321, p)
+q = S.make_queries(db, 400, 1322, p, peaks=(20, 150),
+                   window_mix=[(0.5, "ppm", 10.0), (0.3, "da", 50.0), (0.2, "da", 500.0)])
+ix = dslim.Index(p)
+ix.construct_all(db)
+lib = ix.lib
+d = _dev(q)
+n, npk = q.nspec, int(q.moz.shape[0])
+outs = [_out(n) for _ in range(4)]
+ref_out, ref_hist = _out(n)
+torch.cuda.synchronize()
+free = []
+shapes = [dict(schedule=0), dict(schedule=2, pairs_per_warp=4, threads=512), dict(schedule=0, pairs_per_warp=8, threads=512),
+          dict(schedule=1, pairs_per_warp=1)]
+for k, (o, h) in enumerate(outs):
+    ix.set_tuning(**shapes[k])
+    rc = lib.hc_dslim_query_noalloc(ix.ctx, *_args(d, n, npk, o, h), None)
+    assert rc == 0, lib.hc_last_error(ix.ctx)
+    torch.cuda.synchronize()
+    free.append(torch.cuda.mem_get_info()[0])
+ix.set_tuning(schedule=0)
+rc = lib.hc_dslim_query_device(ix.ctx, *_args(d, n, npk, ref_out, ref_hist), None)
+assert rc == 0, lib.hc_last_error(ix.ctx)
+torch.cuda.synchronize()
+r_ref, h_ref = _results(ref_out, ref_hist, n)
+rep = 0
+for o, h in outs:
+    r, hh = _results(o, h, n)
+    rep = compare(r, hh, r_ref, h_ref)["reported"]
+ix.close()
+print("RESULT " + json.dumps({"free": free, "reported": rep}))
+"""
+
+
+def test_noalloc_first_call_in_fresh_process_then_no_allocation():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _CHILD, root], capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-3000:]
+    line = [x for x in r.stdout.splitlines() if x.startswith("RESULT ")][-1]
+    out = json.loads(line[7:])
+    free = out["free"]
+    # after the set-up call (free[0]) no call changed the free device memory
+    assert all(f == free[0] for f in free[1:]), free
+    assert out["reported"] > 0
