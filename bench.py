@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "spectra/s & postings GB/s vs HBM peak: batched+learned vs plain GPU, same PSMs"
 WORKLOAD = os.environ.get("HC_WORKLOAD", "open-2m")
-CPU_SAMPLE = int(os.environ.get("HC_CPU_SAMPLE", "2000"))
+CPU_SAMPLE = int(os.environ.get("HC_CPU_SAMPLE", "10000"))
 
 
 def log(*a):
@@ -209,6 +209,20 @@ def next_rows(ix, p, q, res):
     return out
 
 
+def port_speed() -> dict | None:
+    """The oracle port's speed against the reference's own DSLIM query compiled unmodified,
+    measured where the reference sources exist (oracle/time_port_vs_ref.py)."""
+    path = os.path.join(ROOT, "oracle", "port_vs_reference.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    c = d.get("cases", {})
+    return {"measured_on": f"{d.get('host')} with {d.get('threads')} threads",
+            "port_vs_reference_speed": {k: round(v["port_vs_reference_speed"], 3) for k, v in c.items()},
+            "meaning": "port spectra/s / reference spectra/s on the same workload and threads (>1: port faster)"}
+
+
 def cpu_baseline(p, db, q, threads: int, sample: int):
     """The oracle (CPU restatement of DSLIM_QuerySpectrum) on a bounded sample."""
     from oracle import oracle as O
@@ -222,23 +236,31 @@ def cpu_baseline(p, db, q, threads: int, sample: int):
     dt = time.perf_counter() - t
     return {"value": qs.nspec / dt, "unit": "spectra/s", "cores": threads, "kind": "port",
             "sample": f"first {qs.nspec} spectra of the {q.nspec}-spectrum batch, one pass, "
-                      f"{dt:.1f}s wall"}, ref
+                      f"{dt:.1f}s wall", "port_vs_reference": port_speed()}, ref
 
 
 def parity_sample(gpu, ref) -> dict:
-    """GPU results (expeRT e-values) against the oracle on the same spectra: integer
-    fields bit-exact, hyperscore within 1e-5 relative, |log10 e| within 0.05."""
+    """GPU results against the oracle on the same spectra: integer fields bit-exact,
+    hyperscore within 1e-5 relative, |log10 e| within 0.05 for every spectrum (those
+    whose e-value came from the learned tail are reported apart as well)."""
     k = ref.shape[0]
     g = gpu[:k]
     exact = {f: int((g[f] != ref[f]).sum()) for f in ("cpsms", "idxoffset", "psid", "sharedions", "reported",
                                                       "post_bytes")}
     h = np.abs(g["hyperscore"].astype(np.float64) - ref["hyperscore"]) > 1e-5 * np.abs(ref["hyperscore"]) + 1e-30
     both = (g["evalue"] > 0) & (ref["evalue"] > 0) & (ref["reported"] == 1)
-    de = np.abs(np.log10(g["evalue"][both]) - np.log10(ref["evalue"][both])) if both.any() else np.zeros(1)
+    lrn = both & ((g["flags"] & 0x200) != 0)
+    fit = both & ~lrn
+    de = np.zeros(k)
+    de[both] = np.abs(np.log10(g["evalue"][both]) - np.log10(ref["evalue"][both]))
+    fit_ok = not (de[fit] > 0.05).any()
+    lst = dlog_stats(de[lrn])
     return {"spectra": int(k), "mismatches_exact": exact, "hyperscore_over_1e-5": int(h.sum()),
-            "evalues_compared": int(both.sum()), "dlog10e_max": float(de.max()),
-            "evalue_over_0.05": int((de > 0.05).sum()),
-            "identical": bool(not any(exact.values()) and not h.any() and not (de > 0.05).any())}
+            "evalues_compared": int(both.sum()),
+            "expeRT_fit": {"spectra": int(fit.sum()), "dlog10e_max": float(de[fit].max()) if fit.any() else 0.0,
+                           "over_0.05": int((de[fit] > 0.05).sum())},
+            "learned": {"spectra": int(lrn.sum()), **lst},
+            "identical": bool(not any(exact.values()) and not h.any() and fit_ok and lst["over_0.05"] == 0)}
 
 
 def run_reference(args, rank, world, dist):
@@ -267,7 +289,8 @@ def run_reference(args, rank, world, dist):
                       "dF_bins": p.dF, "dM_da": p.dM, "maxz": p.maxz, "mods": "M+15.99 <=2"},
            "impl": "reference",
            "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": threads, "kind": "port",
-                            "sample": f"{per_step} spectra per step of the 100k-spectrum batch"},
+                            "sample": f"{per_step} spectra per step of the 100k-spectrum batch",
+                            "port_vs_reference": port_speed()},
            "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -352,28 +375,60 @@ def run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning):
             "same_psms": mism == 0, "psm_field_mismatches": mism, "batched_tuning": best}
 
 
-def learned_stats(m, d_X, res0, mode: int, thresh: float = 0.1) -> dict:
-    """Learned e-values of one mode for spectra whose expeRT results are res0 (host),
-    with features d_X (device, n x 256): learned share of the reported spectra,
-    fallback rate and |log10 e - log10 e_expeRT| percentiles over the learned ones."""
+def dlog_stats(dl: np.ndarray) -> dict:
+    """Percentiles of |log10 e - log10 e_expeRT| over learned spectra."""
+    if dl.size == 0:
+        dl = np.zeros(1)
+    return {"dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
+            "dlog10e_p99": float(np.percentile(dl, 99)), "dlog10e_max": float(dl.max()),
+            "over_0.05": int((dl > 0.05).sum()), "within_0.05": float(np.mean(dl <= 0.05))}
+
+
+def dev_batch(q):
+    """Device buffers of a CSR batch plus result and histogram outputs; returns (tensors, query args)."""
     import torch
+    from hicops_gb300._lib import RESULT_DTYPE, HC_HIST_BINS
+    n = q.nspec
+    d = dict(idx=torch.from_numpy(q.idx.astype(np.int32)).cuda(), moz=torch.from_numpy(q.moz.view(np.int32)).cuda(),
+             inten=torch.from_numpy(q.intensity.view(np.int32)).cuda(), prec=torch.from_numpy(q.precurse).cuda(),
+             dM=None if q.dM is None else torch.from_numpy(q.dM).cuda(),
+             out=torch.empty(max(1, n) * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda"),
+             hist=torch.empty(max(1, n) * HC_HIST_BINS, dtype=torch.int32, device="cuda"))
+    a = (d["idx"].data_ptr(), d["moz"].data_ptr(), d["inten"].data_ptr(), d["prec"].data_ptr(),
+         None if d["dM"] is None else d["dM"].data_ptr(), n, int(q.moz.shape[0]), d["out"].data_ptr(),
+         d["hist"].data_ptr())
+    return d, a
+
+
+def dev_results(d, n):
     from hicops_gb300._lib import RESULT_DTYPE
-    n = res0.shape[0]
-    d_res = torch.from_numpy(np.frombuffer(res0.tobytes(), dtype=np.uint8).copy()).cuda()
-    learned = torch.empty(n, dtype=torch.float32, device="cuda")
-    nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
-    scr = torch.empty(n * 3, dtype=torch.float32, device="cuda")
-    m.evalues(d_X.data_ptr(), d_res.data_ptr(), n, thresh, learned.data_ptr(), nfb.data_ptr(), scr.data_ptr(),
-              mode=mode)
+    return np.frombuffer(d["out"].cpu().numpy().tobytes(), dtype=RESULT_DTYPE)[:n].copy()
+
+
+def train_tail(ix, db, p, seed: int, n: int, epochs: int, mix=None, peaks=None):
+    """The learned tail trained on histograms the GPU search produced: a batch of n spectra
+    from the same generator (another seed) searched with expeRT e-values; 75 % train the
+    network, 25 % check it (learned share, agreement with expeRT)."""
+    import torch
+    from hicops_gb300 import dslim
+    from hicops_gb300 import synthetic as S
+    t = time.time()
+    kw = {}
+    if mix:
+        kw["window_mix"] = mix
+    if peaks:
+        kw["peaks"] = peaks
+    qt = S.make_queries(db, n, seed, p, **kw)
+    d, a = dev_batch(qt)
+    ix.query_device(*a)
     torch.cuda.synchronize()
-    r1 = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=RESULT_DTYPE)
-    ok = (res0["reported"] == 1) & (res0["evalue"] > 0)
-    used = ((r1["flags"] & 0x200) != 0) & ok
-    dl = np.abs(np.log10(r1["evalue"][used]) - np.log10(res0["evalue"][used])) if used.any() else np.zeros(1)
-    return {"mode": mode, "reported": int(ok.sum()), "learned_share": float(used.sum() / max(1, ok.sum())),
-            "fallback_rate": float(1 - used.sum() / max(1, ok.sum())),
-            "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
-            "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
+    ncal = n // 4
+    m, rep = dslim.fit_learned_tail(ix, d["hist"], d["out"], n, np.arange(0, n - ncal), np.arange(n - ncal, n),
+                                    seed=5, epochs=epochs, batch=512)
+    rep["batch_spectra"] = n
+    rep["prepare_s"] = time.time() - t
+    del d
+    return m, rep
 
 
 def learned_tail_1m(ix, p, db):
@@ -381,10 +436,11 @@ def learned_tail_1m(ix, p, db):
     search itself produces. Spectra come from the open-2m generator; each gets a
     target candidate count drawn log-uniform in [10^2, 10^6] and the precursor window
     (+-dM Da) that holds that many entries around its precursor mass (bisection on the
-    sorted entry masses of all lengths; achieved percentiles reported). The search runs in sub-batches
-    of 100,000 (expeRT e-values); 80 % of the spectra train the network with the
-    project's own kernels, the other 20 % are held out: there the learned e-values
-    (fallback to expeRT where the refit residual exceeds 0.1) are compared with expeRT's."""
+    sorted entry masses of all lengths; achieved percentiles reported). The search runs in
+    sub-batches of 100,000 (expeRT e-values); 80 % of the spectra train the network with
+    the project's own kernels and the last 20 % are held out: there the learned tail
+    decides which spectra it takes (predicted residual within 0.1 and a confirmed
+    first bin) and their e-values are compared with expeRT's (the judge)."""
     import torch
     from hicops_gb300 import dslim
     from hicops_gb300 import synthetic as S
@@ -394,86 +450,94 @@ def learned_tail_1m(ix, p, db):
     nb = (N + B - 1) // B
     ntrain = int(0.8 * N)
     rng = np.random.default_rng(0xC31)
-    dX = torch.empty(N * 256, dtype=torch.float32, device="cuda")
-    dY = torch.empty(N * 3, dtype=torch.float32, device="cuda")
     dR = torch.empty(N * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    m = dslim.MLP(ix, seed=0xC32)
+    dH = torch.empty(N * HC_HIST_BINS, dtype=torch.int32, device="cuda")
     t_search = t_gen = 0.0
     counts, wins = [], []
     allm = np.sort(np.concatenate([ix.entries(L)["mass"].astype(np.float64)
                                    for L in range(p.min_len, p.max_len + 1)]))
     cnt = lambda pm, dm: np.searchsorted(allm, pm + dm, "right") - np.searchsorted(allm, pm - dm, "left")
-    try:
-        for b in range(nb):
-            n = min(B, N - b * B)
-            t = time.time()
-            q = S.make_queries(db, n, 0xC31 + 7919 * b, p)
-            target = 10.0 ** rng.uniform(2.0, 6.0, n)
-            pm = q.precurse.astype(np.float64)
-            lo, hi = np.zeros(n), np.full(n, float(p.max_mass))
-            for _ in range(40):
-                mid = 0.5 * (lo + hi)
-                small = cnt(pm, mid) < target
-                lo, hi = np.where(small, mid, lo), np.where(small, hi, mid)
-            q.dM = hi
-            counts.append(cnt(pm, hi))
-            wins.append(hi)
-            t_gen += time.time() - t
-            d = dict(idx=torch.from_numpy(q.idx.astype(np.int32)).cuda(), moz=torch.from_numpy(q.moz.view(np.int32)).cuda(),
-                     inten=torch.from_numpy(q.intensity.view(np.int32)).cuda(), prec=torch.from_numpy(q.precurse).cuda(),
-                     dM=torch.from_numpy(q.dM).cuda(), hist=torch.empty(n * HC_HIST_BINS, dtype=torch.int32, device="cuda"))
-            o = b * B
-            out = dR[o * RESULT_DTYPE.itemsize:(o + n) * RESULT_DTYPE.itemsize]
-            torch.cuda.synchronize()
-            t = time.time()
-            ix.query_device(d["idx"].data_ptr(), d["moz"].data_ptr(), d["inten"].data_ptr(), d["prec"].data_ptr(),
-                            d["dM"].data_ptr(), n, int(q.moz.shape[0]), out.data_ptr(), d["hist"].data_ptr())
-            torch.cuda.synchronize()
-            t_search += time.time() - t
-            m.features(d["hist"].data_ptr(), out.data_ptr(), n, dX[o * 256:].data_ptr())
-            m.targets(out.data_ptr(), n, dY[o * 3:].data_ptr())
-            del d
-        torch.cuda.synchronize()
-        res = np.frombuffer(dR.cpu().numpy().tobytes(), dtype=RESULT_DTYPE).copy()
-        ok = (res["reported"] == 1) & (res["evalue"] > 0)
-        tr = np.nonzero(ok[:ntrain])[0]
-        sel = torch.from_numpy(tr).cuda()
-        Xs, Ys = dX.view(N, 256)[sel].contiguous(), dY.view(N, 3)[sel].contiguous()
-        epochs = int(os.environ.get("HC_L1M_EPOCHS", "20"))
+    for b in range(nb):
+        n = min(B, N - b * B)
         t = time.time()
-        loss = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=2048, epochs=epochs, lr=1e-3)
+        q = S.make_queries(db, n, 0xC31 + 7919 * b, p)
+        target = 10.0 ** rng.uniform(2.0, 6.0, n)
+        pm = q.precurse.astype(np.float64)
+        lo, hi = np.zeros(n), np.full(n, float(p.max_mass))
+        for _ in range(40):
+            mid = 0.5 * (lo + hi)
+            small = cnt(pm, mid) < target
+            lo, hi = np.where(small, mid, lo), np.where(small, hi, mid)
+        q.dM = hi
+        counts.append(cnt(pm, hi))
+        wins.append(hi)
+        t_gen += time.time() - t
+        d, a = dev_batch(q)
+        o = b * B
+        out = dR[o * RESULT_DTYPE.itemsize:(o + n) * RESULT_DTYPE.itemsize]
+        hist = dH[o * HC_HIST_BINS:(o + n) * HC_HIST_BINS]
         torch.cuda.synchronize()
-        t_train = time.time() - t
-        del Xs, Ys
-        Xh = dX[ntrain * 256:]
-        held = {f"mode{k}": learned_stats(m, Xh, res[ntrain:], k) for k in (0, 2)}
-        cc = np.concatenate(counts)
-        return {"histograms": N, "trained_on": int(tr.size), "epochs": epochs, "final_loss": loss,
-                "train_s": t_train, "search_s": t_search, "search_spectra_per_s": N / t_search,
-                "generate_s": t_gen, "windows": "candidate counts log-uniform 1e2-1e6 (window per spectrum)",
-                "window_da_p1_p50_p99": [float(np.percentile(np.concatenate(wins), x)) for x in (1, 50, 99)],
-                "candidates_p1_p50_p99": [float(np.percentile(cc, x)) for x in (1, 50, 99)],
-                "held_out": held}
+        t = time.time()
+        ix.query_device(a[0], a[1], a[2], a[3], a[4], n, a[6], out.data_ptr(), hist.data_ptr())
+        torch.cuda.synchronize()
+        t_search += time.time() - t
+        del d
+    res = np.frombuffer(dR.cpu().numpy().tobytes(), dtype=RESULT_DTYPE).copy()
+    t = time.time()
+    epochs = int(os.environ.get("HC_L1M_EPOCHS", "20"))
+    h0 = ntrain
+    nh = N - h0
+    m, rep = dslim.fit_learned_tail(ix, dH, dR, N, np.arange(0, ntrain), np.arange(h0, N),
+                                    seed=0xC32, epochs=epochs, batch=2048)
+    t_fit = time.time() - t
+    try:
+        # held out: the learned tail's own decision against expeRT
+        r0 = res[h0:]
+        ok = (r0["reported"] == 1) & (r0["evalue"] > 0)
+        X = torch.empty(nh * 256, dtype=torch.float32, device="cuda")
+        hh, rh = dH[h0 * HC_HIST_BINS:], dR[h0 * RESULT_DTYPE.itemsize:]
+        m.features(hh.data_ptr(), rh.data_ptr(), nh, X.data_ptr())
+        used, lg = m.learned_mask(X.data_ptr(), hh.data_ptr(), rh.data_ptr(), nh, r0)
+        dl = np.abs(lg[used] - np.log10(r0["evalue"][used]))
+        held = {"reported": int(ok.sum()), "learned_share": float(used.sum() / max(1, ok.sum())),
+                "fallback_rate": float(1 - used.sum() / max(1, ok.sum())), **dlog_stats(dl)}
     finally:
         m.close()
+    cc = np.concatenate(counts)
+    return {"histograms": N, "fit": rep, "fit_s": t_fit, "search_s": t_search, "search_spectra_per_s": N / t_search,
+            "generate_s": t_gen, "windows": "candidate counts log-uniform 1e2-1e6 (window per spectrum)",
+            "window_da_p1_p50_p99": [float(np.percentile(np.concatenate(wins), x)) for x in (1, 50, 99)],
+            "candidates_p1_p50_p99": [float(np.percentile(cc, x)) for x in (1, 50, 99)],
+            "held_out": held}
 
 
-def run_full(args, rank, world, dist):
+def full_8m(args, rank, world, dist, as_main: bool) -> dict:
     """Config 4: the full pipeline at capacity. 8M peptides + M-ox + N-terminal acetylation
-    (an extension: mod residue code '^') built on the device;
-    1,000,000 spectra of the mixed-window batch streamed from pinned host memory in
-    sub-batches of 50,000 (hc_dslim_query_stream: copies of one sub-batch overlap the
+    (an extension: mod residue code '^') built on the device; spectra of the mixed-window
+    batch (20-150 peaks; 1,000,000 by default) streamed from pinned host memory in
+    sub-batches of 50,000 (hc_dslim_query_stream: the copies of one sub-batch overlap the
     search of the other). Plain: default shape, one CTA per spectrum, expeRT e-values.
-    Batched+learned: autotuned persistent longest-first shape plus the learned tail.
-    Each form is timed over the whole stream (host to host)."""
+    Batched+learned: autotuned persistent longest-first shape plus the learned tail
+    (trained on a separate batch of the same generator). Each form is timed over the
+    whole stream, host to host; the device-resident search of the first sub-batch is
+    timed beside it so the copy overlap shows."""
     import torch
     from hicops_gb300 import dslim
+    from hicops_gb300 import synthetic as S
     from hicops_gb300._lib import RESULT_DTYPE
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    p, db, q = make_workload(rank)
+    p, npep, dbs, nq, qs, kw = S.workload("full-8m")
+    nq = int(os.environ.get("HC_FULL_N", str(nq)))
+    p.threads = os.cpu_count() or 8
+    t = time.time()
+    db = S.make_database(npep, dbs, p)
+    t_db = time.time() - t
+    t = time.time()
+    q = S.make_queries(db, nq, qs + 1000 * rank, p, **kw)
+    t_q = time.time() - t
+    log(f"[bench] full-8m: database {t_db:.1f}s, {q.nspec} spectra {t_q:.1f}s")
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
-    from hicops_gb300 import synthetic as S
     q = S.QueryBatch(idx=pin(q.idx), moz=pin(q.moz), intensity=pin(q.intensity), precurse=pin(q.precurse),
                      charges=q.charges, rtimes=q.rtimes, dM=pin(q.dM))
     t = time.time()
@@ -483,85 +547,89 @@ def run_full(args, rank, world, dist):
     t_build = time.time() - t
     n = q.nspec
     bsz = int(os.environ.get("HC_STREAM_BATCH", "50000"))
-    # plain form
-    ix.set_tuning(schedule=1)
-    plain_tuning = ix.tuning()
-    ix.query_stream(q.slice(0, min(n, 2 * bsz)), bsz)  # warm
-    t = time.perf_counter()
-    r_plain, _, _ = ix.query_stream(q, bsz)
-    t_plain = time.perf_counter() - t
-    # learned tail: trained on histograms this search produced (first sub-batch)
-    qs = q.slice(0, min(n, bsz))
-    d_idx = torch.from_numpy(qs.idx.astype(np.int32)).cuda()
-    d_moz = torch.from_numpy(qs.moz.view(np.int32)).cuda()
-    d_int = torch.from_numpy(qs.intensity.view(np.int32)).cuda()
-    d_prec = torch.from_numpy(qs.precurse).cuda()
-    d_dM = torch.from_numpy(qs.dM).cuda()
-    ns = qs.nspec
-    from hicops_gb300._lib import HC_HIST_BINS
-    d_out = torch.empty(ns * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    d_hist = torch.empty(ns * HC_HIST_BINS, dtype=torch.int32, device="cuda")
-    qa = (d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), d_dM.data_ptr(), ns,
-          int(qs.moz.shape[0]), d_out.data_ptr(), d_hist.data_ptr())
-    ix.query_device(*qa)
-    m = dslim.MLP(ix, seed=5)
-    dX = torch.empty(ns * 256, dtype=torch.float32, device="cuda")
-    dY = torch.empty(ns * 3, dtype=torch.float32, device="cuda")
-    m.features(d_hist.data_ptr(), d_out.data_ptr(), ns, dX.data_ptr())
-    m.targets(d_out.data_ptr(), ns, dY.data_ptr())
-    torch.cuda.synchronize()
-    r0 = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=RESULT_DTYPE)
-    sel = torch.from_numpy(np.nonzero((r0["reported"] == 1) & (r0["evalue"] > 0))[0]).cuda()
-    Xs, Ys = dX.view(ns, 256)[sel].contiguous(), dY.view(ns, 3)[sel].contiguous()
-    m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=512, epochs=20, lr=1e-3)
-    # batched+learned form
-    best, _ = ix.tune_device(*qa[:5], min(ns, 40000), int(qs.idx[min(ns, 40000)]), qa[7], qa[8])
-    ix.set_tuning(**best)
-    ix.query_stream(q.slice(0, min(n, 2 * bsz)), bsz, mlp=m)  # warm
-    t = time.perf_counter()
-    r_b, _, l_b = ix.query_stream(q, bsz, mlp=m)
-    t_b = time.perf_counter() - t
-    fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore")
-    mism = {f: int((r_b[f] != r_plain[f]).sum()) for f in fields}
-    used = (r_b["flags"] & 0x200) != 0
-    ok = (r_plain["reported"] == 1) & (r_plain["evalue"] > 0)
-    dl = np.abs(np.log10(r_b["evalue"][used]) - np.log10(r_plain["evalue"][used])) if used.any() else np.zeros(1)
-    out = {"metric": METRIC, "value": n * world / t_b, "unit": "spectra/s", "n_gpus": world, "steps": 1,
-           "warmup": 1, "ms_per_step": 1000 * t_b, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()),
-                      "entries": int(sum(ix.info(L)[0] for L in range(p.min_len, p.max_len + 1))),
-                      "postings": int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1))),
-                      "spectra": n, "stream_batch": bsz, "peaks": "20-150",
-                      "windows": "50% +-10 ppm, 30% +-50 Da, 20% +-500 Da", "form": "batched+learned",
-                      "tuning": best, "mods": "M+15.99 <=2, N-terminal acetylation <=1 (extension: the reference has no N-terminal mods)"},
-           "plain": {"spectra_per_s": n * world / t_plain, "seconds": t_plain, "tuning": plain_tuning},
-           "speedup_vs_plain": t_plain / t_b, "same_psms_as_plain": not any(mism.values()),
-           "psm_mismatches": mism,
-           "learned": {"learned_share": float(used.sum() / max(1, ok.sum())),
-                       "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
-                       "within_0.05": float(np.mean(dl <= 0.05))},
-           "e2e": {"value": n * world / t_b, "unit": "spectra/s",
-                   "h2d_bytes_per_step": int(q.idx.nbytes + q.moz.nbytes + q.intensity.nbytes + q.precurse.nbytes
-                                             + q.dM.nbytes),
-                   "d2h_bytes_per_step": int(n * RESULT_DTYPE.itemsize + 4 * n)},
-           "index_build_s": t_build}
-    if rank == 0 and not args.no_cpu:
-        try:
-            cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8, int(os.environ.get("HC_CPU_SAMPLE", "1000")))
-            out["cpu_baseline"] = cb
-            out["parity_vs_oracle"] = parity_sample(r_plain, ref)
-        except Exception as e:
-            out["cpu_baseline"] = {"value": None, "error": str(e)}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
-    m.close()
-    ix.close()
+    out = {}
+    try:
+        # plain form
+        ix.set_tuning(schedule=1)
+        plain_tuning = ix.tuning()
+        ix.query_stream(q.slice(0, min(n, 2 * bsz)), bsz)  # warm (and sizes the staging slots)
+        t = time.perf_counter()
+        r_plain, _, _ = ix.query_stream(q, bsz)
+        t_plain = time.perf_counter() - t
+        # device-resident plain search of one sub-batch (no copies)
+        qs1 = q.slice(0, min(n, bsz))
+        d1, a1 = dev_batch(qs1)
+        ix.query_device(*a1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ix.query_device(*a1)
+        torch.cuda.synchronize()
+        t_dev_plain = time.perf_counter() - t
+        # learned tail from a separate batch; batched+learned form
+        m, fit = train_tail(ix, db, p, qs + 7777, 50000, 20, mix=kw.get("window_mix"), peaks=kw.get("peaks"))
+        ns = min(qs1.nspec, 40000)
+        best, _ = ix.tune_device(a1[0], a1[1], a1[2], a1[3], a1[4], ns, int(qs1.idx[ns]), a1[7], a1[8])
+        ix.set_tuning(**best)
+        ix.query_stream(q.slice(0, min(n, 2 * bsz)), bsz, mlp=m)  # warm
+        t = time.perf_counter()
+        r_b, _, _ = ix.query_stream(q, bsz, mlp=m)
+        t_b = time.perf_counter() - t
+        ix.query_learned(m, *a1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ix.query_learned(m, *a1)
+        torch.cuda.synchronize()
+        t_dev_b = time.perf_counter() - t
+        del d1
+        m.close()
+        fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore", "post_bytes")
+        mism = {f: int((r_b[f] != r_plain[f]).sum()) for f in fields}
+        used = (r_b["flags"] & 0x200) != 0
+        ok = (r_plain["reported"] == 1) & (r_plain["evalue"] > 0)
+        dl = np.abs(np.log10(r_b["evalue"][used]) - np.log10(r_plain["evalue"][used]))
+        out = {"spectra": n, "stream_batch": bsz, "peptides": sum(v.shape[0] for v in db.values()),
+               "entries": int(sum(ix.info(L)[0] for L in range(p.min_len, p.max_len + 1))),
+               "postings": int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1))),
+               "index_build_s": t_build, "peaks": "20-150",
+               "windows": "50% +-10 ppm, 30% +-50 Da, 20% +-500 Da",
+               "mods": "M+15.99 <=2, N-terminal acetylation <=1 (extension: the reference has no N-terminal mods)",
+               "plain_streamed_spectra_per_s": n * world / t_plain,
+               "batched_learned_streamed_spectra_per_s": n * world / t_b,
+               "speedup_vs_plain": t_plain / t_b,
+               "device_resident_first_batch": {"spectra": qs1.nspec, "plain_spectra_per_s": qs1.nspec / t_dev_plain,
+                                               "batched_learned_spectra_per_s": qs1.nspec / t_dev_b},
+               "same_psms_as_plain": not any(mism.values()), "psm_mismatches": mism,
+               "learned": {"learned_share": float(used.sum() / max(1, ok.sum())), **dlog_stats(dl)},
+               "fit": fit, "tuning": best, "plain_tuning": plain_tuning,
+               "h2d_bytes": int(q.idx.nbytes + q.moz.nbytes + q.intensity.nbytes + q.precurse.nbytes + q.dM.nbytes),
+               "d2h_bytes": int(n * RESULT_DTYPE.itemsize)}
+        if rank == 0 and not args.no_cpu:
+            try:
+                cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8,
+                                       int(os.environ.get("HC_FULL_CPU_SAMPLE", "1000")))
+                out["cpu_baseline"] = cb
+                out["parity_vs_oracle"] = parity_sample(r_b, ref)
+            except Exception as e:
+                out["cpu_baseline"] = {"value": None, "error": str(e)[:300]}
+    finally:
+        ix.close()
+    if as_main and rank == 0:
+        v = out["batched_learned_streamed_spectra_per_s"]
+        line = {"metric": METRIC, "value": v, "unit": "spectra/s", "n_gpus": world, "steps": 1, "warmup": 1,
+                "ms_per_step": 1000.0 * n * world / v, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": {"workload": "full-8m", "form": "batched+learned, streamed host to host"},
+                "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": out["h2d_bytes"],
+                        "d2h_bytes_per_step": out["d2h_bytes"]},
+                "full_8m": out}
+        print(json.dumps(line), flush=True)
+    return out
 
 
 def run_gpu(args, rank, world, dist):
     import torch
     from hicops_gb300 import dslim
+    from hicops_gb300 import synthetic as S
     from hicops_gb300._lib import RESULT_DTYPE, HC_HIST_BINS
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -573,22 +641,13 @@ def run_gpu(args, rank, world, dist):
     t_build = time.time() - t
     log(f"[bench] device index built in {t_build:.1f}s")
     n = q.nspec
-    npk = int(q.moz.shape[0])
-    # device-resident inputs and outputs
-    d_idx = torch.from_numpy(q.idx.astype(np.int32)).cuda()
-    d_moz = torch.from_numpy(q.moz.view(np.int32)).cuda()
-    d_int = torch.from_numpy(q.intensity.view(np.int32)).cuda()
-    d_prec = torch.from_numpy(q.precurse).cuda()
-    d_out = torch.empty(n * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    d_hist = torch.empty(n * HC_HIST_BINS, dtype=torch.int32, device="cuda")
+    d, qargs = dev_batch(q)
     stream = torch.cuda.Stream()
-    qargs = (d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), None, n, npk,
-             d_out.data_ptr(), d_hist.data_ptr())
-    results = lambda: np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=RESULT_DTYPE).copy()
+    results = lambda: dev_results(d, n)
     ix.set_profiling(True)
 
     def timed(step, k, w, tag):
-        """w untimed steps, then k steps between events on `stream`; per-step k_search ms."""
+        """w untimed steps, then k steps between events on `stream`; median device ms of each stage."""
         with torch.cuda.stream(stream):
             for _ in range(w):
                 step()
@@ -597,12 +656,12 @@ def run_gpu(args, rank, world, dist):
             dist.barrier()
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        kms, launches = [], 0
+        st, launches = [], 0
         torch.cuda.nvtx.range_push(f"timed:{tag}")
         ev0.record(stream)
         for _ in range(k):
             step()
-            kms.append(ix.kernel_times()["search"])  # waits for this step's stage events
+            st.append(ix.stage_times())  # waits for this step's stage events
             launches += ix.last_launch_count()
         ev1.record(stream)
         ev1.synchronize()
@@ -613,139 +672,157 @@ def run_gpu(args, rank, world, dist):
             tt = torch.tensor([ms], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             ms = float(tt.item())
-        return ms, statistics.median(kms), launches
+        med = {key: statistics.median(x[key] for x in st) for key in st[0]}
+        return ms, med, launches
 
-    # ---- plain form: one CTA per spectrum, default launch shape, separate launches, expeRT e-values
+    # ---- plain form: one CTA per spectrum, default launch shape, separate launches, expeRT on every spectrum
     ix.set_tuning(schedule=1)
     plain_tuning = ix.tuning()
-    plain_ms, plain_kms, _ = timed(lambda: ix.query_device(*qargs, stream.cuda_stream),
-                                   max(2, min(args.steps, 3)), 1, "plain")
+    plain_steps = max(2, min(args.steps, 3))
+    plain_ms, plain_st, _ = timed(lambda: ix.query_device(*qargs, stream.cuda_stream), plain_steps, 1, "plain")
     res_plain = results()
     plain_alg = float(res_plain["post_bytes"].sum())
+    plain_value = n * world * plain_steps / (plain_ms / 1000.0)
 
-    # ---- learned part: trained on the histograms this search produced
-    m = dslim.MLP(ix, seed=5)
-    dX = torch.empty(n * 256, dtype=torch.float32, device="cuda")
-    dY = torch.empty(n * 3, dtype=torch.float32, device="cuda")
-    m.features(d_hist.data_ptr(), d_out.data_ptr(), n, dX.data_ptr())
-    m.targets(d_out.data_ptr(), n, dY.data_ptr())
-    torch.cuda.synchronize()
-    ok = (res_plain["reported"] == 1) & (res_plain["evalue"] > 0)
-    sel = torch.from_numpy(np.nonzero(ok)[0][: int(os.environ.get("HC_TRAIN_N", "60000"))]).cuda()
-    Xs, Ys = dX.view(n, 256)[sel].contiguous(), dY.view(n, 3)[sel].contiguous()
-    t = time.time()
-    loss = m.train(Xs.data_ptr(), Ys.data_ptr(), Xs.shape[0], batch=512, epochs=int(os.environ.get("HC_EPOCHS", "20")),
-                   lr=1e-3)
-    t_train = time.time() - t
-    d_learned = torch.empty(n, dtype=torch.float32, device="cuda")
-    d_nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
-    d_scr = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+    # ---- learned tail: trained on the histograms of a separate batch (same generator, other seed)
+    m, fit = train_tail(ix, db, p, 0xC11 + 7777 + 1000 * rank, int(os.environ.get("HC_TRAIN_N", "60000")),
+                        int(os.environ.get("HC_EPOCHS", "30")))
+    d_lg = torch.empty(n, dtype=torch.float32, device="cuda")
 
-    # ---- batched+learned form: autotuned persistent longest-first kernel replayed from a CUDA graph
+    # ---- batched+learned form: autotuned persistent longest-first search and the learned
+    # tail (expeRT only on the spectra its gate sends back), replayed from one CUDA graph
     ns = min(n, 20000)
     t = time.time()
-    best, _ = ix.tune_device(d_idx.data_ptr(), d_moz.data_ptr(), d_int.data_ptr(), d_prec.data_ptr(), None, ns,
-                             int(q.idx[ns]), d_out.data_ptr(), d_hist.data_ptr())
+    best, _ = ix.tune_device(qargs[0], qargs[1], qargs[2], qargs[3], qargs[4], ns, int(q.idx[ns]), qargs[7],
+                             qargs[8])
     t_tune = time.time() - t
     ix.set_tuning(**best)
 
     def step():
-        ix.query_graph(*qargs, stream=stream.cuda_stream)
-        m.features(d_hist.data_ptr(), d_out.data_ptr(), n, dX.data_ptr(), stream.cuda_stream)
-        m.evalues(dX.data_ptr(), d_out.data_ptr(), n, 0.1, d_learned.data_ptr(), d_nfb.data_ptr(),
-                  d_scr.data_ptr(), stream.cuda_stream)
+        ix.query_learned(m, *qargs, d_learned=d_lg.data_ptr(), stream=stream.cuda_stream)
 
     clocks = Clocks(dev) if rank == 0 else None
-    ms, s_ms, launches = timed(step, args.steps, args.warmup, "batched")
+    ms, st, launches = timed(step, args.steps, args.warmup, "batched")
     clk = clocks.stop() if clocks else None
-    launches += 5 * args.steps  # features, three dense layers, learned e-values per step
     res = results()
     alg_bytes = float(res["post_bytes"].sum())
     value = n * world * args.steps / (ms / 1000.0)
     psm_fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore", "post_bytes")
     mismatch = {f: int((res[f] != res_plain[f]).sum()) for f in psm_fields}
     same = not any(mismatch.values())
+    ok = (res_plain["reported"] == 1) & (res_plain["evalue"] > 0)
     used = (res["flags"] & 0x200) != 0
-    dl = np.abs(np.log10(res["evalue"][used]) - np.log10(res_plain["evalue"][used])) if used.any() else np.zeros(1)
-    learned = {"trained_on": int(Xs.shape[0]), "epochs": int(os.environ.get("HC_EPOCHS", "20")),
-               "final_loss": loss, "train_s": t_train, "reported": int(ok.sum()),
-               "learned_share": float(used.sum() / max(1, ok.sum())),
-               "fallback_rate": float(1 - used.sum() / max(1, ok.sum())),
-               "dlog10e_p50": float(np.percentile(dl, 50)), "dlog10e_p90": float(np.percentile(dl, 90)),
-               "dlog10e_p99": float(np.percentile(dl, 99)), "within_0.05": float(np.mean(dl <= 0.05))}
-    try:  # the agreement-gated mode on the same spectra (not timed)
-        learned["mode2"] = learned_stats(m, dX, res_plain, 2)
-    except Exception as e:
-        learned["mode2"] = {"error": str(e)[:200]}
+    fb = ok & ~used
+    dl = np.abs(np.log10(res["evalue"][used]) - np.log10(res_plain["evalue"][used]))
+    learned = {"reported": int(ok.sum()), "learned_share": float(used.sum() / max(1, ok.sum())),
+               "fallback_spectra": int(fb.sum()),
+               "fallback_identical_to_plain": bool(np.array_equal(res[fb].view(np.uint8), res_plain[fb].view(np.uint8))),
+               **dlog_stats(dl),
+               "expeRT_all_spectra_ms": plain_st.get("tailfit"), "learned_tail_ms": st.get("learned"),
+               "tail_ms_saved_per_step": (plain_st.get("tailfit", 0.0) - st.get("learned", 0.0)),
+               "fit": fit}
 
     # ---- uneven batch (mixed precursor windows, 20-150 peaks) on the same index:
     # one plain launch per window class against one batched launch
     mixed = None
     if os.environ.get("HC_MIXED", "1") == "1":
         mixed = run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning)
+    ix.set_tuning(**best)
 
-    # ---- end to end through the host-buffer call (DSLIM_QuerySpectrum's replacement), tuned shape
+    # ---- end to end through the host-buffer calls: the batched+learned form streamed from
+    # pinned host memory (hc_dslim_query_stream with the network; copies of one sub-batch
+    # overlap the search of the other), and the plain host call (hc_dslim_query) beside it
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
-    from hicops_gb300 import synthetic as S
     qh = S.QueryBatch(idx=pin(q.idx), moz=pin(q.moz), intensity=pin(q.intensity), precurse=pin(q.precurse),
                       charges=q.charges, rtimes=q.rtimes)
     ix.set_profiling(False)
-    ix.query(qh, want_hist=False)  # warm the staging buffers
+    e2e_batch = int(os.environ.get("HC_E2E_BATCH", "25000"))
+    ix.query_stream(qh, e2e_batch, mlp=m)  # warm the staging slots
     e2e_t = []
     for _ in range(max(1, min(args.steps, 3))):
         t = time.perf_counter()
-        r2, _ = ix.query(qh, want_hist=False)
+        r2, _, _ = ix.query_stream(qh, e2e_batch, mlp=m)
         e2e_t.append(time.perf_counter() - t)
     e2e = n * world / statistics.median(e2e_t)
-    e2e_same = bool(np.array_equal(r2["psid"], res_plain["psid"]) and np.array_equal(r2["cpsms"], res_plain["cpsms"]))
+    e2e_same = bool(np.array_equal(r2.view(np.uint8), res.view(np.uint8)))
+    ix.query(qh, want_hist=False)
+    t = time.perf_counter()
+    r3, _ = ix.query(qh, want_hist=False)
+    e2e_plain_call = n * world / (time.perf_counter() - t)
     peak, peak_kind = measured_peaks()
+    s_ms = st["search"]
     achieved = alg_bytes / (s_ms / 1000.0) / 1e9
     ratio = traffic_ratio()
     out = {"metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()), "entries": None,
-                      "postings": None, "spectra_per_step": n, "peaks_per_spectrum": int(np.diff(q.idx).max()),
+           "config": {"workload": WORKLOAD, "peptides": sum(v.shape[0] for v in db.values()),
+                      "entries": int(sum(ix.info(L)[0] for L in range(p.min_len, p.max_len + 1))),
+                      "postings": int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1))),
+                      "spectra_per_step": n, "peaks_per_spectrum": int(np.diff(q.idx).max()),
                       "dF_bins": p.dF, "dM_da": p.dM, "maxz": p.maxz, "mods": "M+15.99 <=2",
                       "parallelism": f"replicas{world}",
                       "l2": "index (postings + row table, GBs) larger than L2; no flush",
-                      "form": "batched+learned", "tuning": best},
-           "plain": {"spectra_per_s": n * world * max(2, min(args.steps, 3)) / (plain_ms / 1000.0),
-                     "search_ms": plain_kms, "postings_gbs": plain_alg / (plain_kms / 1000.0) / 1e9,
-                     "frac_of_peak": plain_alg / (plain_kms / 1000.0) / 1e9 / peak, "tuning": plain_tuning},
-           "speedup_vs_plain": value / (n * world * max(2, min(args.steps, 3)) / (plain_ms / 1000.0)),
-           "same_psms_as_plain": bool(same), "psm_mismatches": mismatch, "learned": learned,
-           "mixed_windows": mixed,
+                      "form": "batched+learned (one CUDA graph: search, learned tail, expeRT on the rest)",
+                      "tuning": best},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_source": peak_kind,
                         "traffic": None if ratio is None else ratio * alg_bytes, "kernel": "k_search",
                         "alg_bytes_per_launch": alg_bytes, "kernel_ms": s_ms},
            "e2e": {"value": e2e, "unit": "spectra/s",
                    "h2d_bytes_per_step": int(q.idx.nbytes + q.moz.nbytes + q.intensity.nbytes + q.precurse.nbytes),
-                   "d2h_bytes_per_step": int(n * RESULT_DTYPE.itemsize), "same_results": e2e_same,
-                   "call": "hc_dslim_query (host buffers), tuned launch shape, expeRT e-values"},
-           "gpu_launches": launches, "index_build_s": t_build, "tune_s": t_tune, "clocks": clk}
-    cfg = out["config"]
-    cfg["entries"] = int(sum(ix.info(L)[0] for L in range(p.min_len, p.max_len + 1)))
-    cfg["postings"] = int(sum(ix.info(L)[1] for L in range(p.min_len, p.max_len + 1)))
+                   "d2h_bytes_per_step": int(n * RESULT_DTYPE.itemsize + 4 * n), "same_results": e2e_same,
+                   "call": f"hc_dslim_query_stream (host buffers, sub-batches of {e2e_batch}) with the learned tail",
+                   "plain_host_call_spectra_per_s": e2e_plain_call},
+           "gpu_launches": launches, "index_build_s": t_build, "tune_s": t_tune, "clocks": clk,
+           "stage_ms": st}
     if rank == 0 and not args.no_cpu:
         try:
             cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8, CPU_SAMPLE)
             out["cpu_baseline"] = cb
-            out["parity_vs_oracle"] = parity_sample(res_plain, ref)
+            out["parity_vs_oracle"] = parity_sample(res, ref)
+            out["parity_vs_oracle_plain"] = parity_sample(res_plain, ref)
         except Exception as e:  # the baseline is reported, never required
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0 and os.environ.get("HC_NEXT", "1") == "1":
-        out["next_rows"] = next_rows(ix, p, qh, r2)
+        out["next_rows"] = next_rows(ix, p, qh, r3)
+    m.close()
     if rank == 0 and os.environ.get("HC_LEARNED_1M", "1") == "1":
         try:
             out["learned_tail_1m"] = learned_tail_1m(ix, p, db)
         except Exception as e:
             out["learned_tail_1m"] = {"error": str(e)[:300]}
+    ix.close()
+    del d
+    torch.cuda.empty_cache()
+    if rank == 0 and os.environ.get("HC_FULL", "1") == "1":
+        try:
+            out["full_8m"] = full_8m(args, rank, world, dist, as_main=False)
+        except Exception as e:
+            out["full_8m"] = {"error": str(e)[:300]}
+    # the short summary last, where a truncated tail of the line still holds it
+    l1m = out.get("learned_tail_1m", {}).get("held_out", {})
+    f8 = out.get("full_8m", {})
+    out["plain"] = {"spectra_per_s": plain_value, "search_ms": plain_st["search"],
+                    "tailfit_ms": plain_st.get("tailfit"), "postings_gbs": plain_alg / (plain_st["search"] / 1000.0) / 1e9,
+                    "frac_of_peak": plain_alg / (plain_st["search"] / 1000.0) / 1e9 / peak, "tuning": plain_tuning}
+    out["speedup_vs_plain"] = value / plain_value
+    out["same_psms_as_plain"] = bool(same)
+    out["psm_mismatches"] = mismatch
+    out["learned"] = learned
+    out["summary"] = {
+        "value": value, "plain": plain_value, "speedup_vs_plain": value / plain_value, "same_psms": bool(same),
+        "roofline_frac": achieved / peak, "e2e": e2e,
+        "learned_share": learned["learned_share"], "learned_p99": learned["dlog10e_p99"],
+        "tail_ms_saved_per_step": learned["tail_ms_saved_per_step"],
+        "parity_identical": out.get("parity_vs_oracle", {}).get("identical"),
+        "parity_spectra": out.get("parity_vs_oracle", {}).get("spectra"),
+        "mixed_speedup": None if mixed is None else mixed.get("speedup"),
+        "l1m_learned_share": l1m.get("learned_share"), "l1m_p99": l1m.get("dlog10e_p99"),
+        "full_8m_speedup": f8.get("speedup_vs_plain"), "full_8m_same_psms": f8.get("same_psms_as_plain"),
+        "full_8m_parity_identical": f8.get("parity_vs_oracle", {}).get("identical")}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    m.close()
-    ix.close()
 
 
 def main():
@@ -765,7 +842,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world, dist)
     elif WORKLOAD == "full-8m":
-        run_full(args, rank, world, dist)
+        full_8m(args, rank, world, dist, as_main=True)
     else:
         run_gpu(args, rank, world, dist)
     if dist:

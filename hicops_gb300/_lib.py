@@ -33,6 +33,7 @@ RESULT_DTYPE = np.dtype([
 assert ENTRY_DTYPE.itemsize == 24 and RESULT_DTYPE.itemsize == 64
 
 FLAG_LGFACT_OOB, FLAG_HIST_OOB, FLAG_TAILFIT_OOB, FLAG_TAILFIT_EMPTY, FLAG_WIDE = 1, 2, 4, 8, 0x100
+FLAG_LEARNED = 0x200
 
 
 class HcParams(C.Structure):
@@ -102,7 +103,7 @@ _SIGS = [
     ("hc_ms2_raw", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                              C.c_void_p, C.c_void_p]),
     ("hc_dslim_query_stream", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                        C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                        C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),
     ("hc_dslim_query_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -116,16 +117,19 @@ _SIGS = [
     ("hc_mlp_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
     ("hc_mlp_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
     ("hc_mlp_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
-    ("hc_mlp_targets", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_targets", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("hc_mlp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("hc_mlp_gradients", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                    C.POINTER(C.c_float)]),
     ("hc_mlp_train", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
                                C.POINTER(C.c_float)]),
-    ("hc_mlp_evalues", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_void_p,
-                                 C.c_void_p, C.c_void_p, C.c_void_p]),
-    ("hc_mlp_evalues_mode", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_int, C.c_void_p,
-                                 C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("hc_mlp_set_gate", C.c_int, [C.c_void_p, C.c_float, C.c_uint32]),
+    ("hc_mlp_get_gate", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
+    ("hc_mlp_tail_probe", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("hc_dslim_query_learned", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]),
     ("hc_phase_cycles", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("hc_dslim_query_graph", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -136,6 +140,7 @@ _SIGS = [
     ("hc_tune", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
     ("hc_ctx_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
+    ("hc_last_stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     ("hc_last_kernel_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 ]

@@ -50,7 +50,8 @@ def _cmds(verbose_ptxas: bool = False):
 def _stale(o: str, src: str) -> bool:
     if not os.path.exists(o):
         return True
-    deps = [src, os.path.join(CSRC, "hc_internal.h"), os.path.join(ROOT, "include", "hicops_gb300.h")]
+    deps = [src, os.path.join(ROOT, "include", "hicops_gb300.h")]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     return any(os.path.getmtime(d) > os.path.getmtime(o) for d in deps if os.path.exists(d))
 
 

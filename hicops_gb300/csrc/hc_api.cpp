@@ -172,6 +172,7 @@ int hc_ctx_destroy(hc_ctx *ctx)
         if (e) cudaEventDestroy(e);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    free_stream_stage(ctx->stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HC_SUCCESS;
@@ -437,6 +438,19 @@ int hc_ctx_set_profiling(hc_ctx *ctx, int on)
     if (on && !ctx->ev[0])
         for (auto &e : ctx->ev) HC_CUDA(ctx, cudaEventCreate(&e));
     ctx->profiling = on != 0;
+    return HC_SUCCESS;
+}
+
+int hc_last_stage_times(hc_ctx *ctx, float *ms, int *nstages)
+{
+    if (!ctx || !ms || !nstages) return HC_ERR_INVLD_PTR;
+    if (!ctx->profiling || !ctx->ev[0]) return set_error(ctx, HC_ERR_INVLD_PARAM, "profiling is off");
+    const bool learned = ctx->last_learned;
+    HC_CUDA(ctx, cudaEventSynchronize(ctx->ev[learned ? 5 : 4]));
+    for (int i = 0; i < 4; i++) HC_CUDA(ctx, cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]));
+    ms[4] = 0.0f;
+    if (learned) HC_CUDA(ctx, cudaEventElapsedTime(&ms[4], ctx->ev[4], ctx->ev[5]));
+    *nstages = learned ? 5 : 4;
     return HC_SUCCESS;
 }
 

@@ -11,6 +11,61 @@ namespace hc {
 
 static bool same_key(const GraphKey &a, const GraphKey &b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
 
+// Replays the context's graph for `key`, capturing it first (through `body`
+// on the capture stream) when the key differs from the captured one.
+template <class Body>
+static int replay(hc_ctx *ctx, const GraphKey &key, cudaStream_t st, Body body)
+{
+    if (!ctx->graph_exec || !same_key(key, ctx->graph_key))
+    {
+        if (ctx->graph_exec)
+        {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+        }
+        if (!ctx->cap_stream) HC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        // with profiling on, the stage events are captured as external
+        // event-record nodes (the graph key includes the profiling switch)
+        HC_CUDA(ctx, cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
+        int rc = body(ctx->cap_stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
+        if (rc)
+        {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        HC_CUDA(ctx, e);
+        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        HC_CUDA(ctx, e);
+        ctx->graph_key = key;
+        ctx->graph_launches = ctx->last_launches;
+    }
+    HC_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, st));
+    ctx->last_launches = ctx->graph_launches;
+    return HC_SUCCESS;
+}
+
+static GraphKey make_key(const hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
+                         const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
+                         hc_result *d_out, uint32_t *d_hist)
+{
+    GraphKey key{};
+    key.idx = d_idx;
+    key.moz = d_moz;
+    key.inten = d_intensity;
+    key.prec = d_precurse;
+    key.dM = d_dM;
+    key.out = d_out;
+    key.hist = d_hist;
+    key.nspec = nspec;
+    key.npeaks = npeaks;
+    key.tuning = ctx->tuning;
+    key.profiling = ctx->profiling ? 1u : 0u;
+    return key;
+}
+
 }  // namespace hc
 
 using namespace hc;
@@ -26,47 +81,45 @@ int hc_dslim_query_graph(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
         return set_error(ctx, HC_ERR_INVLD_PTR, "null device buffer");
     cudaSetDevice(ctx->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-    GraphKey key{};
-    key.idx = d_idx;
-    key.moz = d_moz;
-    key.inten = d_intensity;
-    key.prec = d_precurse;
-    key.dM = d_dM;
-    key.out = d_out;
-    key.hist = d_hist;
-    key.nspec = nspec;
-    key.npeaks = npeaks;
-    key.tuning = ctx->tuning;
-    key.profiling = ctx->profiling ? 1u : 0u;
-    if (!ctx->graph_exec || !same_key(key, ctx->graph_key))
-    {
-        if (ctx->graph_exec)
-        {
-            cudaGraphExecDestroy(ctx->graph_exec);
-            ctx->graph_exec = nullptr;
-        }
-        // everything that allocates or copies synchronously happens before capture
-        int rc = prepare_query(ctx, nspec);
-        if (rc) return rc;
-        if (!ctx->cap_stream) HC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
-        // with profiling on, the stage events are captured as external
-        // event-record nodes (the graph key includes the profiling switch)
-        HC_CUDA(ctx, cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
-        rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist,
-                          ctx->cap_stream);
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
-        if (rc) return rc;
-        HC_CUDA(ctx, e);
-        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
-        cudaGraphDestroy(g);
-        HC_CUDA(ctx, e);
-        ctx->graph_key = key;
-        ctx->graph_launches = ctx->last_launches;
-    }
-    HC_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, st));
-    ctx->last_launches = ctx->graph_launches;
-    return HC_SUCCESS;
+    const GraphKey key = make_key(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist);
+    // everything that allocates or copies synchronously happens before capture
+    int rc = prepare_query(ctx, nspec);
+    if (rc) return rc;
+    rc = replay(ctx, key, st, [&](cudaStream_t cs) {
+        return query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist, cs);
+    });
+    ctx->last_learned = false;
+    return rc;
+}
+
+int hc_dslim_query_learned(hc_ctx *ctx, hc_mlp *mlp, const uint32_t *d_idx, const uint32_t *d_moz,
+                           const uint32_t *d_intensity, const float *d_precurse, const double *d_dM, uint32_t nspec,
+                           uint32_t npeaks, hc_result *d_out, uint32_t *d_hist, float *d_learned_log10e,
+                           void *stream)
+{
+    if (!ctx || !mlp) return HC_ERR_INVLD_PTR;
+    if (nspec && (!d_idx || !d_moz || !d_intensity || !d_precurse || !d_out || !d_hist))
+        return set_error(ctx, HC_ERR_INVLD_PTR, "null device buffer");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    GraphKey key = make_key(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist);
+    key.mlp = mlp;
+    key.learned = d_learned_log10e;
+    learned_gate(mlp, &key.gate_resid, &key.gate_radius);
+    int rc = prepare_query(ctx, nspec);
+    if (rc) return rc;
+    if ((rc = learned_prepare(mlp, nspec))) return rc;
+    rc = replay(ctx, key, st, [&](cudaStream_t cs) {
+        int r = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist, cs,
+                             false);
+        if (r) return r;
+        int launches = ctx->last_launches;
+        r = learned_pipeline(mlp, d_hist, d_out, nspec, d_learned_log10e, cs, &launches);
+        ctx->last_launches = launches;
+        return r;
+    });
+    ctx->last_learned = true;
+    return rc;
 }
 
 int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,

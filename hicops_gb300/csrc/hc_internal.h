@@ -126,10 +126,16 @@ struct ScratchPtrs
 struct GraphKey
 {
     const void *idx, *moz, *inten, *prec, *dM, *out, *hist;
+    const void *mlp, *learned;  // the learned form: network, learned log10 e-values (else null)
+    float gate_resid;           // ... and its gate (kernel parameters of the captured graph)
+    uint32_t gate_radius;
     uint32_t nspec, npeaks;
     hc_tuning tuning;
     uint32_t profiling;  // stage events captured or not
 };
+
+struct StreamStage;  // staging slots of hc_dslim_query_stream (hc_stream.cpp)
+void free_stream_stage(StreamStage *s);
 
 struct Launch
 {
@@ -160,13 +166,15 @@ struct hc_ctx
     int last_launches = 0;
     bool lens_dirty = true;
     bool profiling = false;
-    cudaEvent_t ev[5] = {};  // windows | search | wide | tailfit boundaries
+    bool last_learned = false;  // the last query ran the learned tail (stage 5 recorded)
+    cudaEvent_t ev[6] = {};  // windows | search | wide | tailfit | learned tail boundaries
     unsigned long long *d_phase = nullptr;  // per-phase SM cycles of the search kernel (diagnostics)
     double *d_log10 = nullptr;              // log10 table of the exact hyperscore path
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     hc::GraphKey graph_key{};
     int graph_launches = 0;
+    hc::StreamStage *stage = nullptr;  // kept between streaming calls, grown on demand
 };
 
 namespace hc {
@@ -214,14 +222,25 @@ uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads);
 uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm, uint32_t threads);
 int prepare_query(hc_ctx *ctx, uint32_t nspec);
 size_t search_smem(uint32_t tile, uint32_t dF, bool wide, uint32_t threads);
+// tailfit = false leaves the e-values to the learned tail (learned_pipeline)
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
-                 hc_result *d_out, uint32_t *d_hist, cudaStream_t stream);
+                 hc_result *d_out, uint32_t *d_hist, cudaStream_t stream, bool tailfit = true);
+// profiling: stage event i on st (a graph node when st is capturing)
+cudaError_t record_stage(hc_ctx *ctx, int i, cudaStream_t st);
+int tailfit_list(hc_ctx *ctx, hc_result *d_out, const uint32_t *d_hist, const uint32_t *list,
+                 const uint32_t *d_nlist, uint32_t nmax, cudaStream_t st);
 int sync_lengths(hc_ctx *ctx);
 int preload_query_kernels(hc_ctx *ctx);
 int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                          const float *d_prec, const double *d_dM, uint32_t nspec, hc_result *d_out,
                          uint32_t *d_hist, const ScratchPtrs &s, cudaStream_t st);
+
+// hc_mlp.cu: the learned tail after a search without tail fit
+int learned_prepare(hc_mlp *m, uint32_t n);
+void learned_gate(const hc_mlp *m, float *max_resid, uint32_t *radius);
+int learned_pipeline(hc_mlp *m, const uint32_t *d_hist, hc_result *d_res, uint32_t n, float *lg, cudaStream_t st,
+                     int *launches);
 
 int set_error(hc_ctx *ctx, int code, const std::string &msg);
 int cuda_check(hc_ctx *ctx, cudaError_t e, const char *what);

@@ -32,6 +32,7 @@
 #include <cstdio>
 #include <type_traits>
 
+#include "hc_device.cuh"
 #include "hc_internal.h"
 
 namespace hc {
@@ -89,13 +90,6 @@ __device__ __forceinline__ float exact_h(const QueryConst *__restrict__ qc, uint
     h = __dadd_rn(h, ly);
     h = __dadd_rn(h, -6.0);
     return __double2float_rn(h);
-}
-
-// histogram bin (int)(h*10 + 0.5): a float product, then a double sum
-__device__ __forceinline__ int hist_bin(float hf)
-{
-    const float t = __fmul_rn(hf, 10.0f);
-    return (int)__dadd_rn((double)t, 0.5);
 }
 
 template <bool WIDE>
@@ -1045,28 +1039,17 @@ __global__ void k_windows(const LenDev *__restrict__ lens, uint32_t nlen, const 
 }
 
 // ---- tail fit + e-value ------------------------------------------------------
-__device__ __forceinline__ int32_t x86_d2i(double v)
-{
-    // cvttsd2si semantics of the reference's double -> int conversions
-    if (!(v > -2147483649.0 && v < 2147483648.0)) return (int32_t)0x80000000u;
-    return (int32_t)v;
-}
-
 constexpr int kTfWarps = 4;
 
-// One warp per spectrum. Elementwise steps run across lanes; the sums whose
-// rounding depends on order (ybar, top, bot of LinearFit) run on lane 0 in
-// the reference's order. Cumulative sums are exact integers either way.
-__global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict__ out,
-                                                          const uint32_t *__restrict__ hist,
-                                                          uint32_t nspec, uint32_t min_cpsm,
-                                                          double expect_max, int32_t *__restrict__ fitstart)
+// expeRT::ModelTailFit (expeRT.cpp:572-718) and e(x) (dslim_query.cpp:773-799)
+// of spectrum s, by one warp. Elementwise steps run across lanes; the sums
+// whose rounding depends on order (ybar, top, bot of LinearFit) run on lane 0
+// in the reference's order. Cumulative sums are exact integers either way.
+// sx: the warp's HC_HIST_BINS + 2 doubles of shared memory.
+__device__ void tailfit_one(uint32_t s, hc_result *__restrict__ out, const uint32_t *__restrict__ hist,
+                            uint32_t min_cpsm, double expect_max, int32_t *__restrict__ fitstart, double *sx,
+                            int lane)
 {
-    __shared__ double sxs[kTfWarps][HC_HIST_BINS + 2];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t s = blockIdx.x * kTfWarps + warp;
-    if (s >= nspec) return;
-    double *sx = sxs[warp];  // sx[0] stands for index -1; element i is sx[i + 1]
     hc_result r = out[s];
     r.mu = r.beta = r.minhyp = r.nexthyp = r.maxhyp = 0;
     r.evalue = 0.0;
@@ -1084,27 +1067,9 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
     const uint32_t *yy = hist + (size_t)s * HC_HIST_BINS;
     const int hyp = hist_bin(r.hyperscore);  // maxhypscore (dslim_query.cpp:778)
     const int cps = (int)r.cpsms;
-    // expeRT.cpp:590-598: end1 = last bin below hyp holding >= 1, stt1 = first.
-    // Bins past the end exist only when the reference writes out of bounds
-    // (flagged HC_FLAG_HIST_OOB); they read as empty here.
-    int end1 = hyp - 1;
-    for (int q0 = min(hyp - 1, HC_HIST_BINS - 1); q0 >= 0; q0 -= 32)
-    {
-        const int q = q0 - lane;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, q >= 0 && yy[q] >= 1u);
-        if (b) { end1 = q0 - (__ffs(b) - 1); break; }
-    }
-    int stt1 = 0;
-    for (int q0 = 0; q0 <= end1 && q0 < HC_HIST_BINS; q0 += 32)
-    {
-        const int q = q0 + lane;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, q <= end1 && q < HC_HIST_BINS && yy[q] >= 1u);
-        if (b) { stt1 = q0 + __ffs(b) - 1; break; }
-    }
-    if (stt1 == end1) end1 += 1;
-    int n = end1 - stt1 + 1;
-    if (n < 0) n = 0;
-    if (stt1 + n > HC_HIST_BINS) n = HC_HIST_BINS - stt1;
+    // expeRT.cpp:590-598: end1 = last bin below hyp holding >= 1, stt1 = first
+    int stt1, end1;
+    const int n = tail_bins(yy, hyp, HC_HIST_BINS, lane, stt1, end1);
     double mu_t = 0.0, beta_t = 0.0;
     uint32_t fl = 0;
     if (n == 0)
@@ -1212,22 +1177,44 @@ __global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict
             }
         }
     }
-    if (lane != 0) return;
-    fitstart[s] = fit_first;
-    r.flags |= fl;
-    r.mu = x86_d2i(__dmul_rn(mu_t, 1e6));
-    r.beta = x86_d2i(__dmul_rn(beta_t, 1e6));
-    r.minhyp = stt1;
-    r.nexthyp = end1;
-    r.maxhyp = hyp;
-    // e(x) = 10^(w*maxhyp + b) * cpsms (dslim_query.cpp:786-799)
-    const double wv = __ddiv_rn((double)r.mu, 1e6), bv = __ddiv_rn((double)r.beta, 1e6);
-    const double lgs = __dadd_rn(__dmul_rn(wv, (double)hyp), bv);
-    double e = pow(10.0, lgs);
-    e = __dmul_rn(e, (double)r.cpsms);
-    r.evalue = e;
-    r.reported = e < expect_max ? 1u : 0u;
-    out[s] = r;
+    if (lane == 0)
+    {
+        fitstart[s] = fit_first;
+        r.flags |= fl;
+        r.mu = x86_d2i(__dmul_rn(mu_t, 1e6));
+        r.beta = x86_d2i(__dmul_rn(beta_t, 1e6));
+        r.minhyp = stt1;
+        r.nexthyp = end1;
+        r.maxhyp = hyp;
+        // e(x) = 10^(w*maxhyp + b) * cpsms (dslim_query.cpp:786-799)
+        const double wv = __ddiv_rn((double)r.mu, 1e6), bv = __ddiv_rn((double)r.beta, 1e6);
+        const double lgs = __dadd_rn(__dmul_rn(wv, (double)hyp), bv);
+        double e = pow(10.0, lgs);
+        e = __dmul_rn(e, (double)r.cpsms);
+        r.evalue = e;
+        r.reported = e < expect_max ? 1u : 0u;
+        out[s] = r;
+    }
+}
+
+// One warp per spectrum: every spectrum of [0, nspec), or those of `list`
+// (its length *nlist read on the device) when a list is given.
+__global__ void __launch_bounds__(kTfWarps * 32) k_tailfit(hc_result *__restrict__ out,
+                                                          const uint32_t *__restrict__ hist,
+                                                          uint32_t nspec, uint32_t min_cpsm,
+                                                          double expect_max, int32_t *__restrict__ fitstart,
+                                                          const uint32_t *__restrict__ list,
+                                                          const uint32_t *__restrict__ nlist)
+{
+    __shared__ double sxs[kTfWarps][HC_HIST_BINS + 2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *sx = sxs[warp];  // sx[0] stands for index -1; element i is sx[i + 1]
+    const uint32_t cnt = list ? min(*nlist, nspec) : nspec;
+    for (uint32_t w = blockIdx.x * kTfWarps + warp; w < cnt; w += gridDim.x * kTfWarps)
+    {
+        tailfit_one(list ? list[w] : w, out, hist, min_cpsm, expect_max, fitstart, sx, lane);
+        __syncwarp();
+    }
 }
 
 // ---- longest-first order for the batched schedule --------------------------
@@ -1290,7 +1277,7 @@ static uint32_t fit_tile(size_t budget, uint32_t dF, uint32_t threads)
 
 // Stage timing event; inside a stream capture it becomes an external event
 // record node, so a replayed graph still times its stages.
-static cudaError_t record_stage(hc_ctx *ctx, int i, cudaStream_t st)
+cudaError_t record_stage(hc_ctx *ctx, int i, cudaStream_t st)
 {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     const cudaError_t e = cudaStreamIsCapturing(st, &cs);
@@ -1405,12 +1392,13 @@ static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need)
 
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
-                 hc_result *d_out, uint32_t *d_hist, cudaStream_t st)
+                 hc_result *d_out, uint32_t *d_hist, cudaStream_t st, bool tailfit)
 {
     (void)npeaks;
     int rc = sync_lengths(ctx);
     if (rc) return rc;
     ctx->last_launches = 0;
+    ctx->last_learned = !tailfit;
     if (nspec == 0) return HC_SUCCESS;
     const uint32_t nlen = (uint32_t)ctx->lens.size();
     QueryScratch &q = ctx->qs;
@@ -1482,9 +1470,14 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
     if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 3, st));
-    k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
-                                                                            ctx->p.expect_max, q.d_fitstart);
-    HC_CUDA(ctx, cudaGetLastError());
+    if (tailfit)
+    {
+        k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(
+            d_out, d_hist, nspec, ctx->p.min_cpsm, ctx->p.expect_max, q.d_fitstart, nullptr, nullptr);
+        HC_CUDA(ctx, cudaGetLastError());
+    }
+    else
+        launches--;
     if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 4, st));
     ctx->last_launches = launches;
     return HC_SUCCESS;
@@ -1533,6 +1526,22 @@ int preload_query_kernels(hc_ctx *ctx)
     chk(load_one(k_search<false, 8>));
     chk(load_one(k_search<true, 2>));
     HC_CUDA(ctx, e);
+    return HC_SUCCESS;
+}
+
+// The expeRT tail fit of the spectra in `list` (its length *d_nlist on the
+// device, at most nmax): the fallback of the learned tail.
+int tailfit_list(hc_ctx *ctx, hc_result *d_out, const uint32_t *d_hist, const uint32_t *list,
+                 const uint32_t *d_nlist, uint32_t nmax, cudaStream_t st)
+{
+    if (nmax == 0) return HC_SUCCESS;
+    QueryScratch &q = ctx->qs;
+    int rc = grow(ctx, &q.d_fitstart, &q.fit_cap, (size_t)nmax);
+    if (rc) return rc;
+    const uint32_t blocks = std::min<uint32_t>((nmax + kTfWarps - 1) / kTfWarps, (uint32_t)ctx->sm_count * 16);
+    k_tailfit<<<blocks, kTfWarps * 32, 0, st>>>(d_out, d_hist, nmax, ctx->p.min_cpsm, ctx->p.expect_max,
+                                                q.d_fitstart, list, d_nlist);
+    HC_CUDA(ctx, cudaGetLastError());
     return HC_SUCCESS;
 }
 
@@ -1607,7 +1616,8 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true, ctx->tuning.threads), 2, st);
     if (rc) return rc;
     k_tailfit<<<(nspec + kTfWarps - 1) / kTfWarps, kTfWarps * 32, 0, st>>>(d_out, d_hist, nspec, ctx->p.min_cpsm,
-                                                                            ctx->p.expect_max, s.fitstart);
+                                                                            ctx->p.expect_max, s.fitstart, nullptr,
+                                                                            nullptr);
     HC_CUDA(ctx, cudaGetLastError());
     ctx->last_launches = launches + 1;
     return HC_SUCCESS;

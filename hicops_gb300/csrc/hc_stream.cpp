@@ -5,11 +5,17 @@
 // device searches sub-batch b, the host packs sub-batch b+1 into pinned memory
 // and its copies run on a copy stream; results come back on the same copy
 // stream once the search event of their sub-batch has fired.
+//
+// The slots (pinned host and device buffers, the copy stream, events) belong
+// to the context and are kept between calls; a call grows them only when its
+// sub-batches need more room than an earlier call's did.
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "hc_internal.h"
+
+namespace hc {
 
 namespace {
 
@@ -21,8 +27,8 @@ struct Slot
     double *h_dM = nullptr;
     hc_result *h_out = nullptr;
     // device buffers
-    uint32_t *d_idx = nullptr, *d_moz = nullptr, *d_int = nullptr, *d_hist = nullptr, *d_nfb = nullptr;
-    float *d_prec = nullptr, *d_X = nullptr, *d_scr = nullptr, *d_learned = nullptr;
+    uint32_t *d_idx = nullptr, *d_moz = nullptr, *d_int = nullptr, *d_hist = nullptr;
+    float *d_prec = nullptr, *d_learned = nullptr;
     double *d_dM = nullptr;
     hc_result *d_out = nullptr;
     cudaEvent_t ev_in = nullptr, ev_done = nullptr, ev_out = nullptr;
@@ -44,10 +50,7 @@ void free_slot(Slot &s)
     cudaFree(s.d_moz);
     cudaFree(s.d_int);
     cudaFree(s.d_hist);
-    cudaFree(s.d_nfb);
     cudaFree(s.d_prec);
-    cudaFree(s.d_X);
-    cudaFree(s.d_scr);
     cudaFree(s.d_learned);
     cudaFree(s.d_dM);
     cudaFree(s.d_out);
@@ -64,9 +67,93 @@ cudaError_t dmem(T **p, size_t n) { return cudaMalloc((void **)p, sizeof(T) * (n
 
 }  // namespace
 
+struct StreamStage
+{
+    Slot slot[2];
+    cudaStream_t cs = nullptr;  // copy stream
+    // what the slots hold room for
+    uint32_t batch = 0, peaks = 0;
+    bool dM = false, hist = false, learned = false;
+};
+
+void free_stream_stage(StreamStage *st)
+{
+    if (!st) return;
+    for (Slot &s : st->slot) free_slot(s);
+    if (st->cs) cudaStreamDestroy(st->cs);
+    delete st;
+}
+
+// Makes the context's slots hold sub-batches of `batch` spectra and `peaks`
+// peaks with the optional buffers asked for; reallocates only when they do not.
+static int ensure_stage(hc_ctx *ctx, uint32_t batch, uint32_t peaks, bool dM, bool hist, bool learned)
+{
+    StreamStage *&g = ctx->stage;
+    if (g && g->batch >= batch && g->peaks >= peaks && (g->dM || !dM) && (g->hist || !hist) &&
+        (g->learned || !learned))
+        return HC_SUCCESS;
+    StreamStage want;
+    if (g)
+    {
+        want.batch = g->batch;
+        want.peaks = g->peaks;
+        want.dM = g->dM;
+        want.hist = g->hist;
+        want.learned = g->learned;
+        free_stream_stage(g);
+        g = nullptr;
+    }
+    StreamStage *n = new StreamStage();
+    n->batch = std::max(want.batch, batch);
+    n->peaks = std::max(want.peaks, peaks);
+    n->dM = want.dM || dM;
+    n->hist = want.hist || hist;
+    n->learned = want.learned || learned;
+    cudaError_t e = cudaStreamCreateWithFlags(&n->cs, cudaStreamNonBlocking);
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    const size_t B = n->batch, P = n->peaks;
+    for (Slot &s : n->slot)
+    {
+        chk(hpin(&s.h_idx, B + 1));
+        chk(hpin(&s.h_moz, P));
+        chk(hpin(&s.h_int, P));
+        chk(hpin(&s.h_prec, B));
+        chk(hpin(&s.h_out, B));
+        chk(dmem(&s.d_idx, B + 1));
+        chk(dmem(&s.d_moz, P + 4));
+        chk(dmem(&s.d_int, P + 4));
+        chk(dmem(&s.d_prec, B));
+        chk(dmem(&s.d_out, B));
+        chk(dmem(&s.d_hist, B * HC_HIST_BINS));
+        if (n->dM)
+        {
+            chk(hpin(&s.h_dM, B));
+            chk(dmem(&s.d_dM, B));
+        }
+        if (n->hist) chk(hpin(&s.h_hist, B * HC_HIST_BINS));
+        if (n->learned)
+        {
+            chk(hpin(&s.h_learned, B));
+            chk(dmem(&s.d_learned, B));
+        }
+        chk(cudaEventCreateWithFlags(&s.ev_in, cudaEventDisableTiming));
+        chk(cudaEventCreateWithFlags(&s.ev_done, cudaEventDisableTiming));
+        chk(cudaEventCreateWithFlags(&s.ev_out, cudaEventDisableTiming));
+    }
+    if (e != cudaSuccess)
+    {
+        free_stream_stage(n);
+        return set_error(ctx, HC_ERR_BAD_MEM_ALLOC, std::string("stream staging: ") + cudaGetErrorString(e));
+    }
+    g = n;
+    return HC_SUCCESS;
+}
+
+}  // namespace hc
+
 extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uint32_t *moz, const uint32_t *intensity,
                                      const float *precurse, const double *dM_per_spec, uint32_t nspec,
-                                     uint32_t batch, hc_mlp *mlp, float thresh, hc_result *out, uint32_t *hist,
+                                     uint32_t batch, hc_mlp *mlp, hc_result *out, uint32_t *hist,
                                      float *learned_log10e)
 {
     using namespace hc;
@@ -76,7 +163,7 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
     if (batch == 0) return set_error(ctx, HC_ERR_INVLD_SIZE, "hc_dslim_query_stream: batch of 0 spectra");
     for (uint32_t i = 0; i < nspec; i++)
         if (idx[i + 1] < idx[i]) return set_error(ctx, HC_ERR_INVLD_SIZE, "idx not monotone");
-    cudaSetDevice(ctx->device);
+    HC_CUDA(ctx, cudaSetDevice(ctx->device));
     batch = std::min(batch, nspec);
     const uint32_t nb = (nspec + batch - 1) / batch;
     uint32_t maxpk = 0;
@@ -85,50 +172,18 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
         const uint32_t s0 = b * batch, s1 = std::min(nspec, s0 + batch);
         maxpk = std::max(maxpk, idx[s1] - idx[s0]);
     }
-
-    Slot slot[2];
-    cudaStream_t cs = nullptr;
-    int rc = HC_SUCCESS;
+    const bool want_learned = mlp && learned_log10e;
+    int rc = ensure_stage(ctx, batch, maxpk, dM_per_spec != nullptr, hist != nullptr, want_learned);
+    if (rc) return rc;
+    if ((rc = prepare_query(ctx, batch))) return rc;
+    if (mlp && (rc = learned_prepare(mlp, batch))) return rc;
+    StreamStage &g = *ctx->stage;
+    Slot *slot = g.slot;
+    cudaStream_t cs = g.cs;
     auto fail = [&](int code, const char *what) {
         if (rc == HC_SUCCESS) rc = set_error(ctx, code, what);
         return rc;
     };
-    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return fail(HC_ERR_CUDA, "copy stream");
-    for (Slot &s : slot)
-    {
-        cudaError_t e = cudaSuccess;
-        auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-        chk(hpin(&s.h_idx, batch + 1));
-        chk(hpin(&s.h_moz, maxpk));
-        chk(hpin(&s.h_int, maxpk));
-        chk(hpin(&s.h_prec, batch));
-        chk(hpin(&s.h_out, batch));
-        if (dM_per_spec) chk(hpin(&s.h_dM, batch));
-        if (hist) chk(hpin(&s.h_hist, (size_t)batch * HC_HIST_BINS));
-        if (mlp && learned_log10e) chk(hpin(&s.h_learned, batch));
-        chk(dmem(&s.d_idx, batch + 1));
-        chk(dmem(&s.d_moz, maxpk + 4));
-        chk(dmem(&s.d_int, maxpk + 4));
-        chk(dmem(&s.d_prec, batch));
-        chk(dmem(&s.d_out, batch));
-        chk(dmem(&s.d_hist, (size_t)batch * HC_HIST_BINS));
-        if (dM_per_spec) chk(dmem(&s.d_dM, batch));
-        if (mlp)
-        {
-            chk(dmem(&s.d_X, (size_t)batch * 256));
-            chk(dmem(&s.d_scr, (size_t)batch * 3));
-            chk(dmem(&s.d_learned, batch));
-            chk(dmem(&s.d_nfb, 1));
-        }
-        chk(cudaEventCreateWithFlags(&s.ev_in, cudaEventDisableTiming));
-        chk(cudaEventCreateWithFlags(&s.ev_done, cudaEventDisableTiming));
-        chk(cudaEventCreateWithFlags(&s.ev_out, cudaEventDisableTiming));
-        if (e != cudaSuccess)
-        {
-            fail(HC_ERR_BAD_MEM_ALLOC, cudaGetErrorString(e));
-            break;
-        }
-    }
     // results of a finished sub-batch: pinned staging -> the caller's arrays
     auto drain = [&](Slot &s) {
         if (s.s0 < 0) return;
@@ -137,7 +192,7 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
         {
             std::memcpy(out + s.s0, s.h_out, sizeof(hc_result) * s.n);
             if (hist) std::memcpy(hist + (size_t)s.s0 * HC_HIST_BINS, s.h_hist, 4ull * HC_HIST_BINS * s.n);
-            if (s.h_learned) std::memcpy(learned_log10e + s.s0, s.h_learned, 4ull * s.n);
+            if (want_learned) std::memcpy(learned_log10e + s.s0, s.h_learned, 4ull * s.n);
         }
         s.s0 = -1;
     };
@@ -166,14 +221,11 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
             fail(HC_ERR_CUDA, cudaGetErrorString(e));
             break;
         }
-        int q = query_device(ctx, s.d_idx, s.d_moz, s.d_int, s.d_prec, s.d_dM, n, np, s.d_out, s.d_hist,
-                             ctx->stream);
+        int q = query_device(ctx, s.d_idx, s.d_moz, s.d_int, s.d_prec, dM_per_spec ? s.d_dM : nullptr, n, np,
+                             s.d_out, s.d_hist, ctx->stream, mlp == nullptr);
         if (q == HC_SUCCESS && mlp)
-        {
-            q = hc_mlp_features(ctx, s.d_hist, s.d_out, n, s.d_X, ctx->stream);
-            if (q == HC_SUCCESS)
-                q = hc_mlp_evalues(mlp, s.d_X, s.d_out, n, thresh, s.d_learned, s.d_nfb, s.d_scr, ctx->stream);
-        }
+            q = learned_pipeline(mlp, s.d_hist, s.d_out, n, want_learned ? s.d_learned : nullptr, ctx->stream,
+                                 nullptr);
         if (q != HC_SUCCESS)
         {
             rc = q;
@@ -184,7 +236,7 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
         if (e == cudaSuccess) e = cudaMemcpyAsync(s.h_out, s.d_out, sizeof(hc_result) * n, cudaMemcpyDeviceToHost, cs);
         if (e == cudaSuccess && hist)
             e = cudaMemcpyAsync(s.h_hist, s.d_hist, 4ull * HC_HIST_BINS * n, cudaMemcpyDeviceToHost, cs);
-        if (e == cudaSuccess && s.h_learned)
+        if (e == cudaSuccess && want_learned)
             e = cudaMemcpyAsync(s.h_learned, s.d_learned, 4ull * n, cudaMemcpyDeviceToHost, cs);
         if (e == cudaSuccess) e = cudaEventRecord(s.ev_out, cs);
         if (e != cudaSuccess)
@@ -196,12 +248,18 @@ extern "C" int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uin
         s.n = n;
     }
     // the last one or two sub-batches, in order
-    if (slot[0].s0 >= 0 && slot[1].s0 >= 0 && slot[1].s0 < slot[0].s0) std::swap(slot[0], slot[1]);
-    drain(slot[0]);
-    drain(slot[1]);
+    if (slot[0].s0 >= 0 && slot[1].s0 >= 0 && slot[1].s0 < slot[0].s0)
+    {
+        drain(slot[1]);
+        drain(slot[0]);
+    }
+    else
+    {
+        drain(slot[0]);
+        drain(slot[1]);
+    }
     cudaStreamSynchronize(ctx->stream);
     cudaStreamSynchronize(cs);
-    for (Slot &s : slot) free_slot(s);
-    cudaStreamDestroy(cs);
+    slot[0].s0 = slot[1].s0 = -1;
     return rc;
 }

@@ -139,7 +139,7 @@ class Index:
                                            res.shape[0], L.ptr(prec), L.ptr(chg), L.ptr(rt), int(append)),
                     "hc_write_psms")
 
-    def query_stream(self, q, batch: int, mlp=None, thresh: float = 0.1, want_hist: bool = False):
+    def query_stream(self, q, batch: int, mlp=None, want_hist: bool = False):
         """Streams a host batch through the device in sub-batches (DSLIM_SearchManager's
         batch loop, dslim_query.cpp:160-420); returns (results, hist, learned log10 e)."""
         n = q.nspec
@@ -153,7 +153,7 @@ class Index:
         dM = None if getattr(q, "dM", None) is None else np.ascontiguousarray(q.dM, dtype=np.float64)
         self._check(self.lib.hc_dslim_query_stream(
             self.ctx, L.ptr(idx), L.ptr(moz), L.ptr(inten), L.ptr(prec), L.ptr(dM), n, batch,
-            None if mlp is None else mlp.h, C.c_float(thresh), L.ptr(out), L.ptr(hist), L.ptr(learned)),
+            None if mlp is None else mlp.h, L.ptr(out), L.ptr(hist), L.ptr(learned)),
             "hc_dslim_query_stream")
         return out, hist, learned
 
@@ -176,6 +176,14 @@ class Index:
         t = [C.c_float() for _ in range(4)]
         self._check(self.lib.hc_last_kernel_times(self.ctx, *[C.byref(x) for x in t]), "hc_last_kernel_times")
         return dict(zip(("windows", "search", "wide", "tailfit"), (x.value for x in t)))
+
+    def stage_times(self) -> dict:
+        """Device ms of each stage of the last query (profiling on), with the learned tail if it ran."""
+        t = (C.c_float * 5)()
+        k = C.c_int()
+        self._check(self.lib.hc_last_stage_times(self.ctx, t, C.byref(k)), "hc_last_stage_times")
+        names = ("windows", "search", "wide", "tailfit", "learned")
+        return {names[i]: t[i] for i in range(k.value)}
 
     def identity(self, res: np.ndarray):
         """(seqid, modnum, sites) of each top hit (-1 where none)."""
@@ -335,10 +343,23 @@ Index.phase_cycles = _phase_cycles
 Index.set_phase_timing = _set_phase_timing
 
 
-class MLP:
-    """The learned e-value tail (256 -> 128 -> 64 -> 3), on the device of an Index."""
+def _query_learned(ix: Index, mlp, d_idx, d_moz, d_int, d_prec, d_dM, nspec, npeaks, d_out, d_hist,
+                   d_learned=None, stream=None):
+    """Batched+learned form: search, learned tail and expeRT on the rest, replayed from a CUDA graph."""
+    ix._check(ix.lib.hc_dslim_query_learned(
+        ix.ctx, mlp.h, C.c_void_p(d_idx), C.c_void_p(d_moz), C.c_void_p(d_int), C.c_void_p(d_prec),
+        None if d_dM is None else C.c_void_p(d_dM), nspec, npeaks, C.c_void_p(d_out), C.c_void_p(d_hist),
+        None if d_learned is None else C.c_void_p(d_learned), None if stream is None else C.c_void_p(stream)),
+        "hc_dslim_query_learned")
 
-    N_IN, N_OUT = 256, 3
+
+Index.query_learned = _query_learned
+
+
+class MLP:
+    """The learned e-value tail (256 -> 128 -> 64 -> 4), on the device of an Index."""
+
+    N_IN, N_OUT = 256, 4
 
     def __init__(self, ix: Index, seed: int = 1):
         self.ix = ix
@@ -360,6 +381,14 @@ class MLP:
     def set_params(self, p: np.ndarray):
         p = np.ascontiguousarray(p, np.float32)
         self.ix._check(self.ix.lib.hc_mlp_set_params(self.h, L.ptr(p)), "hc_mlp_set_params")
+
+    def gate(self) -> tuple[float, int]:
+        r, k = C.c_float(), C.c_uint32()
+        self.ix._check(self.ix.lib.hc_mlp_get_gate(self.h, C.byref(r), C.byref(k)), "hc_mlp_get_gate")
+        return r.value, k.value
+
+    def set_gate(self, max_resid: float = 0.1, radius: int = 4):
+        self.ix._check(self.ix.lib.hc_mlp_set_gate(self.h, C.c_float(max_resid), radius), "hc_mlp_set_gate")
 
     def gradients(self, d_X: int, d_Y: int, n: int):
         g = np.zeros(self.nparams, np.float32)
@@ -383,15 +412,77 @@ class MLP:
                                                    C.c_void_p(d_X), None if stream is None else C.c_void_p(stream)),
                        "hc_mlp_features")
 
-    def targets(self, d_res: int, n: int, d_Y: int, stream: int | None = None):
-        self.ix._check(self.ix.lib.hc_mlp_targets(self.ix.ctx, C.c_void_p(d_res), n, C.c_void_p(d_Y),
-                                                  None if stream is None else C.c_void_p(stream)), "hc_mlp_targets")
+    def targets(self, d_hist: int, d_res: int, n: int, d_Y: int, stream: int | None = None):
+        """Y[n,4] from expeRT's own window: slope, intercept, first bin, residual (NaN: no target)."""
+        self.ix._check(self.ix.lib.hc_mlp_targets(self.ix.ctx, C.c_void_p(d_hist), C.c_void_p(d_res), n,
+                                                  C.c_void_p(d_Y), None if stream is None else C.c_void_p(stream)),
+                       "hc_mlp_targets")
 
-    def evalues(self, d_X: int, d_res: int, n: int, thresh: float, d_learned: int, d_nfb: int, d_scratch: int,
-                stream: int | None = None, mode: int = 0):
-        """Learned e-values (mode 0: network window; mode 1: the same refit from the curve's first bin)."""
-        self.ix._check(self.ix.lib.hc_mlp_evalues_mode(self.h, C.c_void_p(d_X), C.c_void_p(d_res), n,
-                                                       C.c_float(thresh), mode, C.c_void_p(d_learned),
-                                                       C.c_void_p(d_nfb), C.c_void_p(d_scratch),
-                                                       None if stream is None else C.c_void_p(stream)),
-                       "hc_mlp_evalues")
+    def probe(self, d_X: int | None, d_hist: int, d_res: int, n: int, d_learned: int, d_aux: int,
+              baseline: bool = False, stream: int | None = None):
+        """Learned log10 e-values without the residual gate and, per spectrum, {predicted residual,
+        residual, offset of the confirmed first bin} (NaN where no bin was confirmed)."""
+        self.ix._check(self.ix.lib.hc_mlp_tail_probe(self.h, None if d_X is None else C.c_void_p(d_X),
+                                                     C.c_void_p(d_hist), C.c_void_p(d_res), n, int(baseline),
+                                                     C.c_void_p(d_learned), C.c_void_p(d_aux),
+                                                     None if stream is None else C.c_void_p(stream)),
+                       "hc_mlp_tail_probe")
+
+    def learned_mask(self, d_X: int, d_hist: int, d_res: int, n: int, res: np.ndarray):
+        """(learned, log10 e) of the n spectra as the gated learned tail decides them (host arrays)."""
+        import torch
+        lg = torch.empty(n, dtype=torch.float32, device="cuda")
+        aux = torch.empty(3 * n, dtype=torch.float32, device="cuda")
+        self.probe(d_X, d_hist, d_res, n, lg.data_ptr(), aux.data_ptr())
+        torch.cuda.synchronize()
+        lg, aux = lg.cpu().numpy(), aux.cpu().numpy().reshape(n, 3)
+        gres, _ = self.gate()
+        ok = (res["reported"] == 1) & (res["evalue"] > 0)
+        return ok & np.isfinite(lg) & (aux[:, 0] <= gres), lg
+
+
+def fit_learned_tail(ix: Index, d_hist, d_res, n: int, train: np.ndarray, cal: np.ndarray, seed: int = 5,
+                     epochs: int = 30, batch: int = 512, lr: float = 1e-3, max_resid: float = 0.1,
+                     radius: int = 4) -> tuple["MLP", dict]:
+    """Trains the learned tail on histograms the GPU search produced.
+
+    d_hist / d_res: device tensors (torch) of a search with expeRT e-values over
+    n spectra; train / cal: disjoint spectrum indices. The targets are expeRT's
+    own window (first bin), line and residual on every spectrum with a fit;
+    the report gives the learned share and the agreement with expeRT on the
+    `cal` spectra. Returns the network and the report.
+    """
+    import time
+    import torch
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), dtype=L.RESULT_DTYPE)
+    m = MLP(ix, seed=seed)
+    m.set_gate(max_resid, radius)
+    dX = torch.empty(n * 256, dtype=torch.float32, device=d_hist.device)
+    dY = torch.empty(n * 4, dtype=torch.float32, device=d_hist.device)
+    m.features(d_hist.data_ptr(), d_res.data_ptr(), n, dX.data_ptr())
+    m.targets(d_hist.data_ptr(), d_res.data_ptr(), n, dY.data_ptr())
+    torch.cuda.synchronize()
+    Y = dY.view(n, 4).cpu().numpy()
+    train = np.asarray(train, np.int64)
+    train = train[np.isfinite(Y[train, 2])]  # spectra with an expeRT window
+    X2, Y2 = dX.view(n, 256), dY.view(n, 4)
+    tr = torch.from_numpy(train).to(d_hist.device)
+    t0 = time.time()
+    Xt, Yt = X2[tr].contiguous(), Y2[tr].contiguous()
+    loss = m.train(Xt.data_ptr(), Yt.data_ptr(), Xt.shape[0], batch=batch, epochs=epochs, lr=lr)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    del Xt, Yt
+    cal = np.asarray(cal, np.int64)
+    ca = torch.from_numpy(cal).to(d_hist.device)
+    rsel = d_res.view(-1, 64)[ca].contiguous()
+    hsel = d_hist.view(n, -1)[ca].contiguous()
+    Xc = X2[ca].contiguous()
+    used, lg = m.learned_mask(Xc.data_ptr(), hsel.data_ptr(), rsel.data_ptr(), int(cal.size), res[cal])
+    rc = res[cal]
+    ok = (rc["reported"] == 1) & (rc["evalue"] > 0)
+    dl = np.abs(lg[used] - np.log10(rc["evalue"][used])) if used.any() else np.zeros(1)
+    return m, {"trained_on": int(train.size), "checked_on": int(cal.size), "epochs": epochs, "final_loss": loss,
+               "train_s": t_train, "max_resid": max_resid, "radius": radius,
+               "learned_share": float(used.sum() / max(1, ok.sum())), "dlog10e_max": float(dl.max()),
+               "dlog10e_p99": float(np.percentile(dl, 99))}

@@ -57,7 +57,7 @@ extern "C" {
 #define HC_FLAG_TAILFIT_OOB 0x4u   /* tail-fit slice starts at -1 (expeRT.cpp:653,690) */
 #define HC_FLAG_TAILFIT_EMPTY 0x8u /* empty tail-fit slice: 0/0 fit (expeRT.cpp:590-601) */
 #define HC_FLAG_WIDE 0x100u        /* scored by the wide-scorecard kernel */
-#define HC_FLAG_LEARNED 0x200u     /* e-value from the learned tail (hc_mlp_evalues) */
+#define HC_FLAG_LEARNED 0x200u     /* e-value from the learned tail (hc_dslim_query_learned) */
 
 /* gParams fields on the DSLIM path (slm_dsts.h:359-418). dF is in bins
  * ((uint)(tolerance_Da * scale), hicops.cpp:564); dM in Da; mod_mass is scaled
@@ -208,20 +208,38 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
 /* ---- learned e-value tail (no reference counterpart; replaces the
  * per-spectrum regression of expeRT::ModelTailFit, expeRT.cpp:572-718, which
  * stays the fallback and the judge) ----
- * A 256 -> 128 -> 64 -> 3 FP32 MLP mapping a spectrum's histogram (as its log
- * survival curve, bins >= 255 folded) to the tail line (slope, intercept,
- * first regression bin). Parameters: W1[256x128] b1 W2[128x64] b2 W3[64x3] b3. */
+ * A 256 -> 128 -> 64 -> 4 FP32 MLP mapping a spectrum's histogram (as its log
+ * survival curve, bins >= 255 folded) to the tail line (slope, intercept),
+ * the first bin of the regression window and the line's RMS residual.
+ * Parameters: W1[256x128] b1 W2[128x64] b2 W3[64x4] b3. A spectrum whose
+ * predicted residual is within the gate gets its e-value from the network's
+ * window: the predicted first bin is confirmed on the FP32 survival curve
+ * (the bin before the first point at or below expeRT's 22 % level, tested
+ * for the prediction and its neighbours within the radius), the window ends
+ * at expeRT's 87 % cut (expeRT.cpp:646-676), the line is the FP32
+ * least-squares fit over it and e = 10^(line at the top hit) * cpsms. Every
+ * other spectrum gets the expeRT fit. */
 typedef struct hc_mlp hc_mlp;
 int hc_mlp_create(hc_ctx *ctx, uint64_t seed, hc_mlp **out);
 int hc_mlp_destroy(hc_mlp *m);
 int hc_mlp_num_params(void);
 int hc_mlp_get_params(hc_mlp *m, float *host);
 int hc_mlp_set_params(hc_mlp *m, const float *host);
+/* Gate: the largest predicted RMS residual (log10 units; 0.1 by default) of
+ * a learned spectrum, and the radius (0..15, 4 by default) of first bins
+ * tested on either side of the predicted one. */
+int hc_mlp_set_gate(hc_mlp *m, float max_resid, uint32_t radius);
+int hc_mlp_get_gate(const hc_mlp *m, float *max_resid, uint32_t *radius);
 /* X[n,256] from the histograms and results of a query (device buffers). */
 int hc_mlp_features(hc_ctx *ctx, const uint32_t *d_hist, const hc_result *d_res, uint32_t n, float *d_X,
                     void *stream);
-/* Y[n,3] = the expeRT fit (slope, intercept, first bin) of the context's last query. */
-int hc_mlp_targets(hc_ctx *ctx, const hc_result *d_res, uint32_t n, float *d_Y, void *stream);
+/* Y[n,4] = the training targets from expeRT's own window (found by a full
+ * search of the curve): slope, intercept, first bin, RMS residual of the line
+ * over the window; NaN (no target, no loss) where there is no such fit. */
+int hc_mlp_targets(hc_ctx *ctx, const uint32_t *d_hist, const hc_result *d_res, uint32_t n, float *d_Y,
+                   void *stream);
+/* out[n,4] = the network's outputs (scaled: slope x 10, intercept / 4, first
+ * bin / 10, residual x 5). */
 int hc_mlp_forward(hc_mlp *m, const float *d_X, uint32_t n, float *d_out, void *stream);
 /* Gradients of the mean squared error (scaled targets) over one batch, to host. */
 int hc_mlp_gradients(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, float *host_grads,
@@ -229,26 +247,25 @@ int hc_mlp_gradients(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, 
 /* Adam training over [0, n) in minibatches of `batch` for `epochs`. */
 int hc_mlp_train(hc_mlp *m, const float *d_X, const float *d_Y, uint32_t n, uint32_t batch,
                  uint32_t epochs, float lr, float *final_loss);
-/* Learned e-values. The network's third output picks the start of the
- * tail-regression window in place of expeRT's 22 % rule (expeRT.cpp:646-661);
- * the window ends where expeRT's does (the 87 % rule, 662-676) and the line is
- * the least-squares fit of the spectrum's log survival curve (the features)
- * over it. Where that line's RMS residual over the window is within `thresh`
- * (log10 units: the tail is straight there), its e-value replaces the expeRT
- * one in d_res (flag HC_FLAG_LEARNED); elsewhere the
- * expeRT value stays and *d_nfallback counts it. d_learned_log10e[n] gets the
- * learned log10 e-value (NaN where it fell back); d_out_scratch holds n*3
- * floats (the network's outputs). */
-int hc_mlp_evalues(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh,
-                   float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
-/* The same with mode 1: the window starts at the curve's first bin (no
- * network) and no residual test is made; the baseline the network is
- * measured against. Mode 0 is hc_mlp_evalues. Mode 2 is mode 0 with a second
- * test: the network's own predicted tail line (its first two outputs, expeRT's
- * slope and intercept) must agree with the refitted line at the top hit's
- * hyperscore within `thresh` (log10 units), else the expeRT value stays. */
-int hc_mlp_evalues_mode(hc_mlp *m, const float *d_X, hc_result *d_res, uint32_t n, float thresh, int mode,
-                        float *d_learned_log10e, uint32_t *d_nfallback, float *d_out_scratch, void *stream);
+/* Every spectrum's learned log10 e-value with no residual gate and no result
+ * written (NaN where no first bin was confirmed): d_aux[3n] = {predicted
+ * residual, residual of the line, offset of the confirmed first bin from the
+ * prediction}. baseline != 0 uses no network: the search starts at the
+ * curve's first point (d_X unused). */
+int hc_mlp_tail_probe(hc_mlp *m, const float *d_X, const uint32_t *d_hist, const hc_result *d_res, uint32_t n,
+                      int baseline, float *d_learned_log10e, float *d_aux, void *stream);
+/* Batched+learned query: the search (as hc_dslim_query_graph) without the
+ * tail fit, then features, network, learned e-values where the gates pass,
+ * and the expeRT fit (k_tailfit) only on the spectra left over, all captured
+ * once into a CUDA graph and replayed (a call whose buffers, sizes, tuning or
+ * network differ re-captures). Learned spectra carry HC_FLAG_LEARNED and
+ * their line in mu / beta; integer fields equal hc_dslim_query_device's.
+ * d_learned_log10e (optional, nspec floats): learned log10 e-values (NaN where
+ * expeRT's fit was used). */
+int hc_dslim_query_learned(hc_ctx *ctx, hc_mlp *mlp, const uint32_t *d_idx, const uint32_t *d_moz,
+                           const uint32_t *d_intensity, const float *d_precurse, const double *d_dM,
+                           uint32_t nspec, uint32_t npeaks, hc_result *d_out, uint32_t *d_hist,
+                           float *d_learned_log10e, void *stream);
 /* ---- on-disk index (no reference counterpart: the reference rebuilds its
  * index on every run, hicops.cpp:174-260) ----
  * hc_dslim_save writes every built length (entries, sequences, bucket offsets
@@ -315,14 +332,15 @@ int hc_ms2_close(hc_ms2 *m);
  * searches one after another. The host batch (any host memory, CSR as in
  * hc_dslim_query) is cut into sub-batches of `batch` spectra that alternate
  * between two pinned/device staging slots, so the copies of one sub-batch
- * overlap the search of the other. With `mlp` non-null the learned e-values
- * (hc_mlp_evalues, `thresh`) are applied to every sub-batch and
- * learned_log10e (optional, nspec floats) receives them. hist (optional)
- * receives nspec*HC_HIST_BINS counts. Synchronous: returns when every result
- * is in `out`. */
+ * overlap the search of the other. The slots belong to the context and are
+ * kept between calls (grown when a call needs more room). With `mlp`
+ * non-null every sub-batch gets the learned tail (as hc_dslim_query_learned)
+ * and learned_log10e (optional, nspec floats) receives its values. hist
+ * (optional) receives nspec*HC_HIST_BINS counts. Synchronous: returns when
+ * every result is in `out`. */
 int hc_dslim_query_stream(hc_ctx *ctx, const uint32_t *idx, const uint32_t *moz, const uint32_t *intensity,
                           const float *precurse, const double *dM, uint32_t nspec, uint32_t batch,
-                          hc_mlp *mlp, float thresh, hc_result *out, uint32_t *hist, float *learned_log10e);
+                          hc_mlp *mlp, hc_result *out, uint32_t *hist, float *learned_log10e);
 /* Diagnostics: with phase timing on, the search kernel adds up SM clock
  * cycles per phase (bucket setup, postings stream, score pass 1, score pass 2,
  * tile clear, rest) over all CTAs, then four counts (tiles, tiles scored by a
@@ -343,6 +361,10 @@ int hc_last_launch_count(const hc_ctx *ctx);
 int hc_ctx_set_profiling(hc_ctx *ctx, int on);
 int hc_last_kernel_times(hc_ctx *ctx, float *ms_windows, float *ms_search, float *ms_wide,
                          float *ms_tailfit);
+/* The same as ms[0..3], plus ms[4] = the learned tail (features, network,
+ * learned e-values and the fallback tail fit) when the last query ran it;
+ * *nstages = 5 then, else 4 (and the tail fit is ms[3]). */
+int hc_last_stage_times(hc_ctx *ctx, float *ms, int *nstages);
 
 #ifdef __cplusplus
 }

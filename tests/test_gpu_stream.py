@@ -44,34 +44,31 @@ def test_stream_matches_oracle(setup):
 
 
 def test_stream_with_learned_evalues(setup):
+    """Streamed sub-batches with the learned tail give exactly what the
+    batched+learned device call gives on the whole batch."""
     import torch
     from hicops_gb300 import dslim
     p, db, q, ix = setup
     n = q.nspec
     d, args = _dev(q)
     ix.query_device(*args)
-    m = dslim.MLP(ix, seed=3)
-    dX = torch.zeros(n * 256, dtype=torch.float32, device="cuda")
-    dY = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
-    m.features(d["hist"].data_ptr(), d["out"].data_ptr(), n, dX.data_ptr())
-    m.targets(d["out"].data_ptr(), n, dY.data_ptr())
     torch.cuda.synchronize()
-    m.train(dX.data_ptr(), dY.data_ptr(), n, batch=256, epochs=20, lr=1e-3)
-    # device path: search, features, learned e-values on the whole batch
-    learned = torch.zeros(n, dtype=torch.float32, device="cuda")
-    nfb = torch.zeros(1, dtype=torch.int32, device="cuda")
-    scratch = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
-    m.evalues(dX.data_ptr(), d["out"].data_ptr(), n, 0.1, learned.data_ptr(), nfb.data_ptr(), scratch.data_ptr())
+    m, rep = dslim.fit_learned_tail(ix, d["hist"], d["out"], n, np.arange(0, n, 2), np.arange(1, n, 2), seed=3,
+                                    epochs=20, batch=256)
+    lg = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    ix.query_learned(m, *args, d_learned=lg.data_ptr())
     torch.cuda.synchronize()
     r0, _ = _results(d, n)
-    # streamed in sub-batches with the same network
-    r1, _, l1 = ix.query_stream(q, 333, mlp=m, thresh=0.1)
+    r1, _, l1 = ix.query_stream(q, 333, mlp=m)
     assert np.array_equal(r0.view(np.uint8), r1.view(np.uint8)), "streamed learned results differ"
-    l0 = learned.cpu().numpy()
-    both = ~np.isnan(l0)
+    l0 = lg.cpu().numpy()
     assert np.array_equal(np.isnan(l0), np.isnan(l1))
+    both = ~np.isnan(l0)
     assert np.array_equal(l0[both], l1[both])
     assert ((r1["flags"] & 0x200) != 0).any()
+    # a second call reuses the context's staging slots and gives the same
+    r2, _, _ = ix.query_stream(q, 333, mlp=m)
+    assert np.array_equal(r1.view(np.uint8), r2.view(np.uint8))
     m.close()
 
 
