@@ -350,17 +350,19 @@ def run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning):
     saved = ix.tuning()
     ix.set_tuning(**plain_tuning)  # schedule 1, default shape
 
-    def plain_step():
-        for (d, a) in dparts:
-            ix.query_device(*a, stream.cuda_stream)
-
-    p_ms, _, _ = timed(plain_step, steps, 1, "mixed_plain")
-    plain_res = [res_of(d, x.nspec) for (d, _), x in zip(dparts, parts)]
+    # one plain launch per window class, each class timed on its own
+    p_cls = []
+    for (dd, aa), x in zip(dparts, parts):
+        ms_c, st_c, _ = timed(lambda: ix.query_device(*aa, stream.cuda_stream), steps, 1, "mixed_plain")
+        p_cls.append({"spectra": x.nspec, "ms": ms_c / steps, "search_ms": st_c["search"],
+                      "spectra_per_s": x.nspec / (ms_c / steps / 1000.0)})
+    p_ms = steps * sum(c["ms"] for c in p_cls)
+    plain_res = [res_of(dd, x.nspec) for (dd, _), x in zip(dparts, parts)]
     ns = min(nm, 40000)
     best, _ = ix.tune_device(afull[0], afull[1], afull[2], afull[3], afull[4], ns, int(qm.idx[ns]),
                              afull[7], afull[8])
     ix.set_tuning(**best)
-    b_ms, _, _ = timed(lambda: ix.query_graph(*afull, stream=stream.cuda_stream), steps, 1, "mixed_batched")
+    b_ms, b_st, _ = timed(lambda: ix.query_graph(*afull, stream=stream.cuda_stream), steps, 1, "mixed_batched")
     res = res_of(dfull, nm)
     fields = ("cpsms", "idxoffset", "psid", "sharedions", "hyperscore")
     mism = 0
@@ -372,6 +374,7 @@ def run_mixed(ix, p, db, rank, world, dist, args, stream, timed, plain_tuning):
     return {"spectra": nm, "classes": {"ppm10": int((cls == 0).sum()), "da50": int((cls == 1).sum()),
                                        "da500": int((cls == 2).sum())},
             "plain_per_class_spectra_per_s": pv, "batched_spectra_per_s": bv, "speedup": bv / pv,
+            "plain_classes": dict(zip(("ppm10", "da50", "da500"), p_cls)), "batched_search_ms": b_st["search"],
             "same_psms": mism == 0, "psm_field_mismatches": mism, "batched_tuning": best}
 
 

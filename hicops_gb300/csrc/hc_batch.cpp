@@ -131,6 +131,8 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     const hc_tuning saved = ctx->tuning;
+    // stage 1: schedule x CTAs per SM x block size x chunks in flight, each with
+    // the largest scorecard tile that fits
     std::vector<hc_tuning> cand;
     for (uint32_t sched : {0u, 2u})
         for (uint32_t cps : {1u, 2u})
@@ -152,16 +154,14 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
     cudaEvent_t e0, e1;
     HC_CUDA(ctx, cudaEventCreate(&e0));
     HC_CUDA(ctx, cudaEventCreate(&e1));
-    float best_t = 1e30f;
-    hc_tuning best_c = saved;
     const bool prof = ctx->profiling;
     ctx->profiling = false;
     int rc = HC_SUCCESS;
-    for (const hc_tuning &t : cand)
-    {
-        if (hc_ctx_set_tuning(ctx, &t) != HC_SUCCESS) continue;
+    std::vector<std::pair<float, hc_tuning>> timed;
+    auto run = [&](const hc_tuning &t) {
+        if (hc_ctx_set_tuning(ctx, &t) != HC_SUCCESS) return;
         rc = query_device(ctx, d_idx, d_moz, d_intensity, d_precurse, d_dM, nspec, npeaks, d_out, d_hist, st);
-        if (rc) break;
+        if (rc) return;
         float ms[2];
         for (int r = 0; r < 2 && !rc; r++)
         {
@@ -171,25 +171,47 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
             cudaEventSynchronize(e1);
             cudaEventElapsedTime(&ms[r], e0, e1);
         }
+        if (!rc) timed.emplace_back(std::min(ms[0], ms[1]), t);
+    };
+    for (const hc_tuning &t : cand)
+    {
+        run(t);
         if (rc) break;
-        const float m = std::min(ms[0], ms[1]);
-        if (m < best_t)
+    }
+    // stage 2: smaller scorecard tiles (fewer candidates per tile, more room for
+    // the shared lists) for the three fastest shapes
+    if (!rc)
+    {
+        std::sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        const size_t top = std::min<size_t>(3, timed.size());
+        std::vector<hc_tuning> more;
+        for (size_t k = 0; k < top; k++)
+            for (uint32_t cut : {1u, 2u, 4u})
+            {
+                hc_tuning t = timed[k].second;
+                if (t.tile <= cut * kRowG) continue;
+                t.tile -= cut * kRowG;
+                more.push_back(t);
+            }
+        for (const hc_tuning &t : more)
         {
-            best_t = m;
-            best_c = t;
+            run(t);
+            if (rc) break;
         }
     }
     ctx->profiling = prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc)
+    if (rc || timed.empty())
     {
         ctx->tuning = saved;
-        return rc;
+        return rc ? rc : set_error(ctx, HC_ERR_INVLD_PARAM, "no launch shape could be timed");
     }
-    ctx->tuning = best_c;
-    if (best) *best = best_c;
-    if (best_ms) *best_ms = best_t;
+    const auto bestp = *std::min_element(timed.begin(), timed.end(),
+                                         [](const auto &a, const auto &b) { return a.first < b.first; });
+    ctx->tuning = bestp.second;
+    if (best) *best = bestp.second;
+    if (best_ms) *best_ms = bestp.first;
     return HC_SUCCESS;
 }
 

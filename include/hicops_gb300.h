@@ -200,8 +200,10 @@ int hc_dslim_query_noalloc(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d
                            const double *d_dM, uint32_t nspec, uint32_t npeaks,
                            hc_result *d_out, uint32_t *d_hist, void *stream);
 /* Autotuner: times the search on a device-resident sample batch for every
- * launch shape of a small grid (block size, tile, lists per warp, CTAs per SM,
- * schedule), keeps the fastest in the context and returns it. */
+ * launch shape of a small grid (schedule x CTAs per SM x block size x chunks
+ * in flight per lane, each with the largest scorecard tile that fits), then
+ * smaller tiles (1, 2 and 4 row-table blocks fewer) for the three fastest,
+ * keeps the fastest in the context and returns it. */
 int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_intensity,
             const float *d_precurse, const double *d_dM, uint32_t nspec, uint32_t npeaks,
             hc_result *d_out, uint32_t *d_hist, hc_tuning *best, float *best_ms);
