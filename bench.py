@@ -778,7 +778,7 @@ def run_gpu(args, rank, world, dist):
                    "call": f"hc_dslim_query_stream (host buffers, sub-batches of {e2e_batch}) with the learned tail",
                    "plain_host_call_spectra_per_s": e2e_plain_call},
            "gpu_launches": launches, "index_build_s": t_build, "tune_s": t_tune, "clocks": clk,
-           "stage_ms": st}
+           "stage_ms": st, "mixed_windows": mixed}
     if rank == 0 and not args.no_cpu:
         try:
             cb, ref = cpu_baseline(p, db, q, os.cpu_count() or 8, CPU_SAMPLE)

@@ -9,7 +9,7 @@ from hicops_gb300 import synthetic as S
 from oracle import oracle as O
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("plain", "mods", "narrow")
+CASES = ("plain", "mods", "narrow", "plain20k")  # plain20k: configs[0] at its full size
 
 
 def crc(a) -> int:
@@ -41,3 +41,11 @@ def load(name: str):
                      charges=np.full(nq, 2, np.int32), rtimes=np.zeros(nq, np.float32))
     rec = {k[4:]: z[k] for k in z.files if k.startswith("rec_")}
     return p, db, q, entries, crcs, rec
+
+
+def hist_matches(hist: np.ndarray, rec: dict, rows: np.ndarray) -> bool:
+    """The histograms of the reported spectra `rows` against the reference's: stored
+    whole for the small cases, as one CRC per spectrum for the full-size one."""
+    if "hist" in rec:
+        return bool(np.array_equal(hist[rows], rec["hist"]))
+    return bool(np.array_equal(np.array([crc(h) for h in hist[rows]], np.uint32), rec["hist_crc"]))

@@ -36,9 +36,19 @@ def crc(a: np.ndarray) -> int:
     return zlib.crc32(np.ascontiguousarray(a).tobytes()) & 0xFFFFFFFF
 
 
+# configs[0] at its full size (20,000 peptides, 2,000 spectra, dF 0.02 Da, dM 100 Da,
+# fragment charges 1-2): the histograms are stored as one CRC per spectrum
+FULL = {"plain20k": "plain-20k"}
+
+
 def make(name: str) -> str:
-    kw, npep, nq, sdb, sq, qkw = CASES[name]
-    p = S.SearchParams(threads=4, **kw)
+    if name in FULL:
+        p, npep, sdb, nq, sq, qkw = S.workload(FULL[name])
+        p.threads = 4
+        kw = {k: getattr(p, k) for k in ("maxz", "dF", "dM")}
+    else:
+        kw, npep, nq, sdb, sq, qkw = CASES[name]
+        p = S.SearchParams(threads=4, **kw)
     db = S.make_database(npep, sdb, p)
     q = S.make_queries(db, nq, sq, p, **qkw)
     r = refrun.run(p, db, q, dump_index=True)
@@ -58,12 +68,13 @@ def make(name: str) -> str:
         ent_mass=ent["mass"], ent_seqid=ent["seqid"], ent_modnum=ent["modnum"], ent_sites=ent["sites"],
         nent=nent, index_crc=crcs,
         **{f"rec_{f}": rec[f] for f in rec.dtype.names if not f.startswith("pad") and f != "hist"},
-        rec_hist=rec["hist"][rec["reported"] == 1])
+        **({"rec_hist_crc": np.array([crc(h) for h in rec["hist"][rec["reported"] == 1]], np.uint32)}
+           if name in FULL else {"rec_hist": rec["hist"][rec["reported"] == 1]}))
     return out
 
 
 if __name__ == "__main__":
     if not refrun.build():
         sys.exit("the reference sources are needed to regenerate the golden vectors")
-    for n in CASES:
+    for n in list(CASES) + list(FULL):
         print(make(n), os.path.getsize(os.path.join(HERE, f"ref_{n}.npz")))

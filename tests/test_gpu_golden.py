@@ -5,12 +5,13 @@ reference byte for byte (CRC). Queries: for every reported spectrum, cpsms,
 histogram, the top hyperscore and tail-fit ints equal the reference's; the top
 hit is the reference's candidate, or (on an exact hyperscore tie, where the
 reference's min-heap decides by insertion order) a candidate with the same
-hyperscore.
+hyperscore. `plain20k` is configs[0] at its full size (20,000 peptides,
+2,000 spectra, dF 0.02 Da, dM 100 Da).
 """
 import numpy as np
 import pytest
 
-from tests._golden import CASES, crc, load
+from tests._golden import CASES, crc, hist_matches, load
 
 pytestmark = pytest.mark.gpu
 
@@ -30,7 +31,7 @@ def test_gpu_matches_reference(name):
     assert np.array_equal(res["reported"] == 1, rep)
     i = np.nonzero(rep)[0]
     assert np.array_equal(res["cpsms"][i], rec["npsms"][i])
-    assert np.array_equal(hist[i], rec["hist"])
+    assert hist_matches(hist, rec, i)
     assert np.array_equal(res["hyperscore"][i], rec["hyperscore"][i])
     assert np.array_equal(res["maxhyp"][i], rec["maxhyp"][i])
     same = (res["psid"][i] == rec["psid"][i]) & (res["idxoffset"][i] == rec["idxoffset"][i])
