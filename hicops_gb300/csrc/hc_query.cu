@@ -38,9 +38,6 @@
 namespace hc {
 namespace {
 
-// Per-tile shared-memory lists, sized from the tile (tiles are multiples of 2048):
-//   chunk -> list map tile/2 (u16), past which a chunk finds its list by search.
-__host__ __device__ constexpr uint32_t cmap_cap(uint32_t tile) { return tile / 2; }
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
 constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two, >= 32 + 64)
 constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
@@ -132,6 +129,7 @@ struct SmemTail
     uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
     uint32_t ndefer;           // undecided candidates queued for the exact evaluation
     uint32_t cchunks[2];       // 16-byte chunks (all lists) of the job in each bound buffer
+    uint32_t ncl[2];           // its non-empty lists
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
@@ -153,8 +151,8 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, cmap, defer, linfo, lend, loff, pmoz, pint, wq, sink, tail, total;
-    uint32_t maxpairs, loffs;  // linfo / loff entries per buffer (two buffers each)
+    size_t qual, defer, linfo, lend, loff, coff, clid, pmoz, pint, wq, sink, tail, total;
+    uint32_t maxpairs, loffs, clids;  // linfo / loff / coff / clid entries per buffer (two buffers each)
 };
 
 __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide, uint32_t nwarps)
@@ -162,14 +160,16 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
     o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
-    o.cmap = o.qual;  // (no per-tile candidate list)
-    o.defer = o.cmap + 2ull * cmap_cap(tile);
+    o.defer = o.qual;
     o.maxpairs = (uint32_t)maxpairs;
     o.loffs = (uint32_t)maxpairs + 4;
+    o.clids = (uint32_t)maxpairs + 8;
     o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
     o.lend = o.linfo + 2 * 8 * maxpairs;  // (maxpairs = 100 (2 dF + 1): every size stays a multiple of 16)
     o.loff = o.lend + 4 * maxpairs;
-    o.pmoz = o.loff + 2 * 4 * (maxpairs + 4);
+    o.coff = o.loff + 2 * 4 * (maxpairs + 4);
+    o.clid = o.coff + 2 * 4 * (maxpairs + 4);
+    o.pmoz = o.clid + 2 * 2 * (maxpairs + 8);
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
     o.sink = (o.wq + 2ull * kWQ * nwarps + 15) & ~(size_t)15;
@@ -275,31 +275,49 @@ __device__ __forceinline__ uint32_t row_hi(const uint32_t *__restrict__ col, uin
     return __ldg(col + (c1 + kRowG - 1) / kRowG);
 }
 
-// Warp-level: exclusive chunk offsets of lists [0, np) in place (lo[np] =
-// total); the total also goes to *total. Must be called by all 32 lanes of a warp.
-__device__ void chunk_offsets(uint32_t *lo, uint32_t np, int lane, uint32_t *total)
+// Warp-level: from the chunk counts lo[0, np) of a job's lists, the job's
+// non-empty lists in order: clid[k] = the list, coff[k] = its first chunk (of
+// all lists laid end to end), coff[ncl] = total. *total and *ncl get the
+// totals. Must be called by all 32 lanes of a warp.
+__device__ void chunk_offsets(const uint32_t *lo, uint32_t np, int lane, uint32_t *coff, uint16_t *clid,
+                              uint32_t *total, uint32_t *ncl)
 {
     const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
-    uint32_t sum = 0;
-    for (uint32_t i = b; i < e; i++) sum += lo[i];
-    uint32_t x = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
-    }
-    uint32_t run = x - sum;
+    uint32_t sum = 0, nz = 0;
     for (uint32_t i = b; i < e; i++)
     {
         const uint32_t t = lo[i];
-        lo[i] = run;
-        run += t;
+        sum += t;
+        nz += t ? 1u : 0u;
+    }
+    uint32_t x = sum, z = nz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o), w = __shfl_up_sync(0xFFFFFFFFu, z, o);
+        if (lane >= o)
+        {
+            x += y;
+            z += w;
+        }
+    }
+    uint32_t run = x - sum, k = z - nz;
+    for (uint32_t i = b; i < e; i++)
+    {
+        const uint32_t t = lo[i];
+        if (t)
+        {
+            coff[k] = run;
+            clid[k] = (uint16_t)i;
+            k++;
+            run += t;
+        }
     }
     if (lane == 31)
     {
-        lo[np] = x;
+        coff[z] = x;
         *total = x;
+        *ncl = z;
     }
 }
 
@@ -384,7 +402,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     const uint32_t nbin = 2 * a.dF + 1;
     const SmemLayout L = smem_layout(tile, a.dF, WIDE, blockDim.x >> 5);
     W *card = reinterpret_cast<W *>(smem);
-    uint16_t *cmap = reinterpret_cast<uint16_t *>(smem + L.cmap);    // chunk -> list
+    uint32_t *coff = reinterpret_cast<uint32_t *>(smem + L.coff);    // per buffer: first chunk of each non-empty list
+    uint16_t *clid = reinterpret_cast<uint16_t *>(smem + L.clid);    // per buffer: which list it is
     uint2 *defer = reinterpret_cast<uint2 *>(smem + L.defer);  // undecided candidates: {b word, y word}
     uint2 *linfo = reinterpret_cast<uint2 *>(smem + L.linfo);  // per list, two buffers: {first, intensity}
     uint32_t *lend = reinterpret_cast<uint32_t *>(smem + L.lend);  // per list: end of the current job's list
@@ -392,7 +411,6 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
-    const uint32_t ccap = cmap_cap(tile);
 
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5;
@@ -570,6 +588,21 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // the block scores job j.
         Job jb = first_job(T.win, a.nlen, tile);
         uint32_t pf_hi[kPf], ps_lo[kPf];
+        // the bucket and the intensity of this thread's lists tid + m * nthr
+        // (list = (valid peak, bin)): the same for every job of the spectrum
+        uint32_t my_bkt[kPf], my_int[kPf];
+#pragma unroll
+        for (int m = 0; m < kPf; m++)
+        {
+            const uint32_t pr = tid + m * nthr;
+            my_bkt[m] = my_int[m] = 0u;
+            if (pr < np)
+            {
+                const uint32_t k = pr / nbin, j = pr - k * nbin;
+                my_bkt[m] = pmoz[k] - a.dF + j;
+                my_int[m] = pint[k];
+            }
+        }
         uint32_t npass = 0;  // postings of entries inside the window (the reference visits exactly these)
         uint32_t cur = 0;
         if (jb.l != kNoJob)
@@ -588,7 +621,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
             }
             __syncthreads();
-            if (wid == 0) chunk_offsets(loff, np, lane, &T.cchunks[0]);
+            if (wid == 0) chunk_offsets(loff, np, lane, coff, clid, &T.cchunks[0], &T.ncl[0]);
         }
         __syncthreads();
         while (jb.l != kNoJob)
@@ -596,30 +629,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             const LenDev d = a.lens[jb.l];
             const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
             uint2 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
-            uint32_t *lo_c = loff + cur * L.loffs, *lo_n = loff + (cur ^ 1) * L.loffs;
+            uint32_t *lo_n = loff + (cur ^ 1) * L.loffs;  // the next job's chunk counts
             const uint32_t C = T.cchunks[cur];
-            // ---- chunk -> list map: each thread a contiguous run of chunks ----
-            {
-                const uint32_t cm = min(C, ccap), per = (cm + nthr - 1) / nthr;
-                const uint32_t k0 = min(cm, (uint32_t)tid * per), k1 = min(cm, k0 + per);
-                if (k0 < k1)
-                {
-                    uint32_t lo = 0, hi = np;  // last list with lo_c[i] <= k0
-                    while (hi - lo > 1)
-                    {
-                        const uint32_t m = (lo + hi) >> 1;
-                        if (lo_c[m] <= k0) lo = m;
-                        else hi = m;
-                    }
-                    uint32_t i = lo;
-                    for (uint32_t k = k0; k < k1; k++)
-                    {
-                        while (lo_c[i + 1] <= k) i++;
-                        cmap[k] = (uint16_t)i;
-                    }
-                }
-            }
-            __syncthreads();
+            const uint32_t ncl = T.ncl[cur];
+            const uint32_t *co = coff + cur * L.loffs;
+            const uint16_t *cl = clid + cur * L.clids;
             HC_PHASE(0);
             // ---- row-table words of the next job's boundaries, in flight ----
             const Job nj = next_job(jb, T.win, a.nlen, tile);
@@ -634,8 +648,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t pr = tid + m * nthr;
                     if (pr < np)
                     {
-                        const uint32_t k = pr / nbin, j = pr - k * nbin;
-                        const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
+                        const uint32_t *col = dn.rows + (size_t)my_bkt[m] * dn.stride;
                         pf_hi[m] = row_hi(col, nj.c1);
                         if (!same) ps_lo[m] = row_lo(col, nj.c0);
                     }
@@ -666,6 +679,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 if (q0 >= C) break;
                 uint4 v[G];
                 uint32_t inte[G];
+                // the list holding chunk q0, then for each group of 32 chunks the
+                // list of every lane's chunk: lists that start inside the group
+                // set one bit each at their first lane, and a lane's list is the
+                // one before plus the bits at or below it
+                uint32_t k0 = find_list(co, ncl, q0, lane);
 #pragma unroll
                 for (int g = 0; g < G; g++)
                 {
@@ -675,23 +693,22 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     v[g] = make_uint4(kQpostPad, kQpostPad, kQpostPad, kQpostPad);
                     if (kb < C)  // warp-uniform
                     {
-                        uint32_t i = 0;
-                        if (kb + 32u > ccap)  // past the map: search
-                            i = find_list(lo_c, np, kb, lane);
+                        const uint32_t j1 = k0 + 1u + (uint32_t)lane;
+                        const uint32_t u = (j1 <= ncl ? co[j1] : 0xFFFFFFFFu) - kb;  // >= 1
+                        const uint32_t msk = __reduce_or_sync(0xFFFFFFFFu, u < 32u ? (1u << u) : 0u);
+                        const uint32_t k = k0 + (uint32_t)__popc(msk & ((2u << lane) - 1u));
                         if (kc < C)
                         {
-                            if (kc < ccap) i = cmap[kc];
-                            else
-                                while (i + 1 < np && lo_c[i + 1] <= kc) i++;
-                            const uint2 li = li_c[i];
+                            const uint2 li = li_c[cl[k]];
                             // a chunk never leaves its bucket (buckets start at
                             // multiples of 4, padded to them); its postings
                             // outside [first, end) belong to entries outside
                             // the tile and fail the index test below
-                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - lo_c[i]);
+                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - co[k]);
                             inte[g] = li.y;
                             v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
                         }
+                        k0 = __shfl_sync(0xFFFFFFFFu, k, 31);  // the list holding chunk kb + 31
                     }
                 }
 #pragma unroll
@@ -765,7 +782,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         const uint32_t st = same ? lend[pr] : ps_lo[m], en = pf_hi[m];
                         if (inter && st < en) npass += en - st;
-                        li_n[pr] = make_uint2(st, pint[pr / nbin]);
+                        li_n[pr] = make_uint2(st, my_int[m]);
                         lend[pr] = en;
                         lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                         prefetch_l2(dn.qp, st, en);
@@ -787,7 +804,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             __syncthreads();
             HC_PHASE(1);
             // ---- the next job's chunk offsets (warp 0, before its scoring share) ----
-            if (wid == 0 && nj.l != kNoJob) chunk_offsets(lo_n, np, lane, &T.cchunks[cur ^ 1]);
+            if (wid == 0 && nj.l != kNoJob)
+                chunk_offsets(lo_n, np, lane, coff + (cur ^ 1) * L.loffs, clid + (cur ^ 1) * L.clids,
+                              &T.cchunks[cur ^ 1], &T.ncl[cur ^ 1]);
             // ---- every candidate that reached min_shp ----
             // cpsms, histogram and the top hit (see score_one). The packed tile
             // is scanned two candidates per lane and step; a warp collects its
@@ -833,14 +852,57 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                 };
                 const uint32_t first = 4 * (tid - (uint32_t)lane), step = 4 * nthr;
+                const uint32_t thr4 = min(a.thr, 255u) * 0x01010101u;
                 for (uint32_t base = first; base < ntile; base += step)
                 {
                     // words past ntile are zero (the tile is cleared after use)
                     const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
                     const uint4 wa = ca < ntile ? c4[ca >> 1] : make_uint4(0u, 0u, 0u, 0u);
                     const uint4 wb = cb < ntile ? c4[cb >> 1] : make_uint4(0u, 0u, 0u, 0u);
-                    push(wa, ca);
-                    push(wb, cb);
+                    // the four candidates' counts (the top bytes of their b and y
+                    // words) summed and compared as bytes: candidates ca, ca + 1,
+                    // cb, cb + 1 in bytes 0..3 (each count < 128, so no carry)
+                    const uint32_t bw = __byte_perm(__byte_perm(wa.x, wa.z, 0x0073u), __byte_perm(wb.x, wb.z, 0x0073u),
+                                                    0x5410u);
+                    const uint32_t yw = __byte_perm(__byte_perm(wa.y, wa.w, 0x0073u), __byte_perm(wb.y, wb.w, 0x0073u),
+                                                    0x5410u);
+                    const uint32_t q = __vcmpgeu4(__vadd4(bw, yw), thr4) & 0x01010101u;
+                    uint32_t m = (q | (q >> 7) | (q >> 14) | (q >> 21)) & 0xFu;
+                    // this lane's place in the warp's ring: an inclusive scan of the counts
+                    const uint32_t n4 = __popc(m);
+                    uint32_t inc = n4;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                        if (lane >= o) inc += t;
+                    }
+                    const uint32_t tot = __shfl_sync(0xFFFFFFFFu, inc, 31);
+                    if (tot == 0) continue;
+                    if (qh + tot <= kWQ)
+                    {
+                        uint32_t r = qhead + qh + inc - n4;
+                        while (m)
+                        {
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1;
+                            wq[r & (kWQ - 1)] = (uint16_t)((k < 2 ? ca : cb) + (uint32_t)(k & 1));
+                            r++;
+                        }
+                        qh += tot;
+                        while (qh >= 32)
+                        {
+                            pop_score(32);
+                            qhead += 32;
+                            qh -= 32;
+                        }
+                    }
+                    else
+                    {
+                        // the ring would overflow: the two halves one after the other
+                        push(wa, ca);
+                        push(wb, cb);
+                    }
                 }
                 if (qh) pop_score(qh);
                 // the warp's own words, now read: clear them for the next job
