@@ -50,7 +50,7 @@ static int check_params(const hc_params *p)
         return HC_ERR_INVLD_PARAM;
     if ((uint64_t)p->max_mass * p->scale >= 0x7FFFFFFFull) return HC_ERR_INVLD_PARAM;
     if (p->nmods > HC_MAX_MODS || p->topmatches > 63) return HC_ERR_INVLD_PARAM;
-    if (p->dF > 16) return HC_ERR_INVLD_PARAM;  // (2dF+1) bins per peak kept in shared memory
+    if (p->dF > 16) return HC_ERR_INVLD_PARAM;  // (2dF+1) bins per peak kept in shared memory (hc_query.cu kMaxDF)
     return HC_SUCCESS;
 }
 

@@ -112,6 +112,17 @@ struct Card<true>
     static constexpr int kWords = 2;
 };
 
+// What the tile loop reads of a length's record, kept in shared memory for
+// the kernel's lifetime (one global read per CTA instead of one per job).
+struct LenS
+{
+    const uint32_t *qp, *rows;
+    uint32_t stride, n;
+};
+
+constexpr uint32_t kMaxDF = 16;  // the largest dF hc_ctx_create accepts
+constexpr uint32_t kMaxGroups = (HC_QALEN * (2 * kMaxDF + 1) + 31) / 32;  // groups of 32 lists
+
 struct SmemTail
 {
     uint32_t hist[HC_HIST_BINS];
@@ -136,6 +147,9 @@ struct SmemTail
     unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations
     int2 win[HC_MAX_LENGTHS];  // the spectrum's window per length
     float lgf[kLgTable];
+    uint32_t gtc[kMaxGroups];  // per group of 32 lists of the next job: chunks
+    uint32_t gtz[kMaxGroups];  // ... and non-empty lists
+    LenS len[HC_MAX_LENGTHS];
 };
 
 // adds the cycles since the last mark to phase k (thread 0 only, after a barrier)
@@ -275,49 +289,60 @@ __device__ __forceinline__ uint32_t row_hi(const uint32_t *__restrict__ col, uin
     return __ldg(col + (c1 + kRowG - 1) / kRowG);
 }
 
-// Warp-level: from the chunk counts lo[0, np) of a job's lists, the job's
-// non-empty lists in order: clid[k] = the list, coff[k] = its first chunk (of
-// all lists laid end to end), coff[ncl] = total. *total and *ncl get the
-// totals. Must be called by all 32 lanes of a warp.
-__device__ void chunk_offsets(const uint32_t *lo, uint32_t np, int lane, uint32_t *coff, uint16_t *clid,
-                              uint32_t *total, uint32_t *ncl)
+// Chunk offsets of a job's lists, in two steps around a block barrier, with
+// the lists in groups of 32 (group g = lists 32g .. 32g + 31).
+// Step 1, by the warp that computed the group's chunk counts (cnt = this
+// lane's list, 0 past the last list): the group's totals of chunks and of
+// non-empty lists.
+__device__ __forceinline__ void group_totals(uint32_t cnt, uint32_t g, int lane, uint32_t *gtc, uint32_t *gtz)
 {
-    const uint32_t per = (np + 31) / 32, b = min(np, (uint32_t)lane * per), e = min(np, b + per);
-    uint32_t sum = 0, nz = 0;
-    for (uint32_t i = b; i < e; i++)
+    const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    const uint32_t z = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, cnt != 0u));
+    if (lane == 0)
     {
-        const uint32_t t = lo[i];
-        sum += t;
-        nz += t ? 1u : 0u;
+        gtc[g] = c;
+        gtz[g] = z;
     }
-    uint32_t x = sum, z = nz;
+}
+
+// Step 2, one warp per group, any warp: from the chunk counts lo[0, np) and
+// the group totals, the job's non-empty lists in order: clid[k] = the list,
+// coff[k] = its first chunk (of all lists laid end to end); the warp of the
+// last group (of ng) writes coff[ncl] = *total and the counts.
+__device__ __forceinline__ void group_offsets(uint32_t g, uint32_t ng, const uint32_t *lo, uint32_t np, int lane,
+                                              const uint32_t *gtc, const uint32_t *gtz, uint32_t *coff,
+                                              uint16_t *clid, uint32_t *total, uint32_t *ncl)
+{
+    uint32_t pc = 0, pz = 0;
+    for (uint32_t i = (uint32_t)lane; i < g; i += 32)
+    {
+        pc += gtc[i];
+        pz += gtz[i];
+    }
+    pc = __reduce_add_sync(0xFFFFFFFFu, pc);
+    pz = __reduce_add_sync(0xFFFFFFFFu, pz);
+    const uint32_t pr = 32 * g + (uint32_t)lane;
+    const uint32_t cnt = pr < np ? lo[pr] : 0u;
+    uint32_t c = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
     {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o), w = __shfl_up_sync(0xFFFFFFFFu, z, o);
-        if (lane >= o)
-        {
-            x += y;
-            z += w;
-        }
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, c, o);
+        if (lane >= o) c += y;
     }
-    uint32_t run = x - sum, k = z - nz;
-    for (uint32_t i = b; i < e; i++)
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, cnt != 0u);
+    if (cnt)
     {
-        const uint32_t t = lo[i];
-        if (t)
-        {
-            coff[k] = run;
-            clid[k] = (uint16_t)i;
-            k++;
-            run += t;
-        }
+        const uint32_t k = pz + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+        coff[k] = pc + c - cnt;
+        clid[k] = (uint16_t)pr;
     }
-    if (lane == 31)
+    if (g + 1 == ng && lane == 31)
     {
-        coff[z] = x;
-        *total = x;
-        *ncl = z;
+        const uint32_t nz = pz + (uint32_t)__popc(bal);
+        coff[nz] = pc + c;
+        *total = pc + c;
+        *ncl = nz;
     }
 }
 
@@ -421,6 +446,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     uint16_t *wq = reinterpret_cast<uint16_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring (tile < 2^16)
 
     for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
+    for (uint32_t l = tid; l < a.nlen; l += nthr)
+    {
+        const LenDev &ld = a.lens[l];
+        T.len[l] = LenS{ld.qp, ld.rows, ld.stride, ld.n};
+    }
     for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
     if (tid == 0)
     {
@@ -605,28 +635,38 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         }
         uint32_t npass = 0;  // postings of entries inside the window (the reference visits exactly these)
         uint32_t cur = 0;
+        const uint32_t nw = (uint32_t)nthr >> 5, ng = (np + 31) >> 5;
         if (jb.l != kNoJob)
         {
             // the first job's boundaries, directly
-            const LenDev d = a.lens[jb.l];
+            const LenS d = T.len[jb.l];
             const bool inter = !WIDE && job_interior(jb, d.n);
-            for (uint32_t pr = tid; pr < np; pr += nthr)
+            for (uint32_t base = 0; base < np; base += (uint32_t)nthr)
             {
-                const uint32_t k = pr / nbin, j = pr - k * nbin;
-                const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
-                const uint32_t st = row_lo(col, jb.c0), en = row_hi(col, jb.c1);
-                if (inter && st < en) npass += en - st;
-                linfo[pr] = make_uint2(st, pint[k]);
-                lend[pr] = en;
-                loff[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                const uint32_t pr = base + (uint32_t)tid;
+                uint32_t cnt = 0;
+                if (pr < np)
+                {
+                    const uint32_t k = pr / nbin, j = pr - k * nbin;
+                    const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
+                    const uint32_t st = row_lo(col, jb.c0), en = row_hi(col, jb.c1);
+                    if (inter && st < en) npass += en - st;
+                    linfo[pr] = make_uint2(st, pint[k]);
+                    lend[pr] = en;
+                    cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                    loff[pr] = cnt;
+                }
+                if (base + 32 * (uint32_t)wid < np) group_totals(cnt, (pr >> 5), lane, T.gtc, T.gtz);
             }
             __syncthreads();
-            if (wid == 0) chunk_offsets(loff, np, lane, coff, clid, &T.cchunks[0], &T.ncl[0]);
+            for (uint32_t g = nw - 1 - (uint32_t)wid; g < ng; g += nw)
+                group_offsets(g, ng, loff, np, lane, T.gtc, T.gtz, coff, clid, &T.cchunks[0], &T.ncl[0]);
+            if (ng == 0 && tid == 0) T.cchunks[0] = T.ncl[0] = coff[0] = 0;
         }
         __syncthreads();
         while (jb.l != kNoJob)
         {
-            const LenDev d = a.lens[jb.l];
+            const LenS d = T.len[jb.l];
             const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
             uint2 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
             uint32_t *lo_n = loff + (cur ^ 1) * L.loffs;  // the next job's chunk counts
@@ -638,10 +678,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             // ---- row-table words of the next job's boundaries, in flight ----
             const Job nj = next_job(jb, T.win, a.nlen, tile);
             const bool same = nj.l == jb.l;
-            LenDev dn;
+            LenS dn;
             if (nj.l != kNoJob)
             {
-                dn = same ? d : a.lens[nj.l];
+                dn = same ? d : T.len[nj.l];
 #pragma unroll
                 for (int m = 0; m < kPf; m++)
                 {
@@ -778,35 +818,50 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 for (int m = 0; m < kPf; m++)
                 {
                     const uint32_t pr = tid + m * nthr;
+                    uint32_t cnt = 0;
                     if (pr < np)
                     {
                         const uint32_t st = same ? lend[pr] : ps_lo[m], en = pf_hi[m];
                         if (inter && st < en) npass += en - st;
                         li_n[pr] = make_uint2(st, my_int[m]);
                         lend[pr] = en;
-                        lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                        cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                        lo_n[pr] = cnt;
                         prefetch_l2(dn.qp, st, en);
                     }
+                    if (m * nthr + 32 * wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
                 }
                 // lists past kPf * nthr (small blocks, wide bin windows): directly
-                for (uint32_t pr = tid + kPf * nthr; pr < np; pr += nthr)
+                for (uint32_t base = kPf * nthr; base < np; base += (uint32_t)nthr)
                 {
-                    const uint32_t k = pr / nbin, j = pr - k * nbin;
-                    const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                    const uint32_t st = same ? lend[pr] : row_lo(col, nj.c0), en = row_hi(col, nj.c1);
-                    if (inter && st < en) npass += en - st;
-                    li_n[pr] = make_uint2(st, pint[k]);
-                    lend[pr] = en;
-                    lo_n[pr] = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                    prefetch_l2(dn.qp, st, en);
+                    const uint32_t pr = base + (uint32_t)tid;
+                    uint32_t cnt = 0;
+                    if (pr < np)
+                    {
+                        const uint32_t k = pr / nbin, j = pr - k * nbin;
+                        const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
+                        const uint32_t st = same ? lend[pr] : row_lo(col, nj.c0), en = row_hi(col, nj.c1);
+                        if (inter && st < en) npass += en - st;
+                        li_n[pr] = make_uint2(st, pint[k]);
+                        lend[pr] = en;
+                        cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
+                        lo_n[pr] = cnt;
+                        prefetch_l2(dn.qp, st, en);
+                    }
+                    if (base + 32 * (uint32_t)wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
                 }
             }
             __syncthreads();
             HC_PHASE(1);
-            // ---- the next job's chunk offsets (warp 0, before its scoring share) ----
-            if (wid == 0 && nj.l != kNoJob)
-                chunk_offsets(lo_n, np, lane, coff + (cur ^ 1) * L.loffs, clid + (cur ^ 1) * L.clids,
-                              &T.cchunks[cur ^ 1], &T.ncl[cur ^ 1]);
+            // ---- the next job's chunk offsets (one group of 32 lists per warp,
+            // the last warps first: the first warps computed the bounds) ----
+            if (nj.l != kNoJob)
+            {
+                for (uint32_t g = nw - 1 - (uint32_t)wid; g < ng; g += nw)
+                    group_offsets(g, ng, lo_n, np, lane, T.gtc, T.gtz, coff + (cur ^ 1) * L.loffs,
+                                  clid + (cur ^ 1) * L.clids, &T.cchunks[cur ^ 1], &T.ncl[cur ^ 1]);
+                if (ng == 0 && tid == 0) T.cchunks[cur ^ 1] = T.ncl[cur ^ 1] = coff[(cur ^ 1) * L.loffs] = 0;
+            }
             // ---- every candidate that reached min_shp ----
             // cpsms, histogram and the top hit (see score_one). The packed tile
             // is scanned two candidates per lane and step; a warp collects its
