@@ -731,7 +731,16 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t kc = kb + (uint32_t)lane;
                     inte[g] = 0u;
                     v[g] = make_uint4(kQpostPad, kQpostPad, kQpostPad, kQpostPad);
-                    if (kb < C)  // warp-uniform
+                    if (kb < C && co[k0 + 1u] >= kb + 32u)  // warp-uniform
+                    {
+                        // the group's 32 chunks all lie in list k0 (most
+                        // postings sit in long lists): one lookup for the warp
+                        const uint2 li = li_c[cl[k0]];
+                        const uint32_t pos = (li.x & ~3u) + 4u * (kc - co[k0]);
+                        inte[g] = li.y;
+                        v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
+                    }
+                    else if (kb < C)  // warp-uniform
                     {
                         const uint32_t j1 = k0 + 1u + (uint32_t)lane;
                         const uint32_t u = (j1 <= ncl ? co[j1] : 0xFFFFFFFFu) - kb;  // >= 1
@@ -908,6 +917,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 };
                 const uint32_t first = 4 * (tid - (uint32_t)lane), step = 4 * nthr;
                 const uint32_t thr4 = min(a.thr, 255u) * 0x01010101u;
+                const bool thr7 = a.thr <= 127u;
                 for (uint32_t base = first; base < ntile; base += step)
                 {
                     // words past ntile are zero (the tile is cleared after use)
@@ -921,8 +931,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                                                     0x5410u);
                     const uint32_t yw = __byte_perm(__byte_perm(wa.y, wa.w, 0x0073u), __byte_perm(wb.y, wb.w, 0x0073u),
                                                     0x5410u);
-                    const uint32_t q = __vcmpgeu4(__vadd4(bw, yw), thr4) & 0x01010101u;
-                    uint32_t m = (q | (q >> 7) | (q >> 14) | (q >> 21)) & 0xFu;
+                    // (a plain add: each sum is below 256). Byte k's top bit of m:
+                    // its sum reaches thr; for thr <= 127, (sum | 0x80) - thr
+                    // keeps the top bit exactly when sum >= thr, with no borrow
+                    // between bytes, and a sum of 128 or more has it already
+                    const uint32_t sw = bw + yw;
+                    uint32_t m = thr7 ? (((sw | 0x80808080u) - thr4) | sw) & 0x80808080u
+                                      : (__vcmpgeu4(sw, thr4) & 0x01010101u) << 7;
                     // this lane's place in the warp's ring: an inclusive scan of the counts
                     const uint32_t n4 = __popc(m);
                     uint32_t inc = n4;
@@ -939,7 +954,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         uint32_t r = qhead + qh + inc - n4;
                         while (m)
                         {
-                            const int k = __ffs(m) - 1;
+                            const int k = (__ffs(m) - 1) >> 3;
                             m &= m - 1;
                             wq[r & (kWQ - 1)] = (uint16_t)((k < 2 ? ca : cb) + (uint32_t)(k & 1));
                             r++;
