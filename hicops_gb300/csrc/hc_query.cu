@@ -40,7 +40,7 @@ namespace {
 
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
 constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two, >= 32 + 64)
-constexpr int kPf = 2;              // lists per thread whose next-job bounds are prefetched
+constexpr int kPf = 2;              // lists per thread whose next-job row-table words are loaded early
 constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
@@ -346,17 +346,6 @@ __device__ __forceinline__ void group_offsets(uint32_t g, uint32_t ng, const uin
     }
 }
 
-// Asks L2 for the 128-byte lines holding postings [st, en) of qp (the 16-byte
-// chunks the stream will read: from st rounded down to a multiple of 4).
-__device__ __forceinline__ void prefetch_l2(const uint32_t *qp, uint32_t st, uint32_t en)
-{
-    if (st >= en) return;
-    const char *p0 = reinterpret_cast<const char *>(qp + (st & ~3u));
-    const char *p1 = reinterpret_cast<const char *>(qp + en);
-    for (const char *p = reinterpret_cast<const char *>((uintptr_t)p0 & ~(uintptr_t)127); p < p1; p += 128)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 // One unit of a spectrum's work: the candidates [c0, c1) of length l, at
 // most one scorecard tile. A window's first tile ends one tile past the
 // window start rounded down to a row-table boundary (kRowG); every later
@@ -614,8 +603,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // per-list bounds are double-buffered:
         // while job j streams, the row-table words of job j+1's boundaries are
         // in flight; right after the stream each thread turns them into job
-        // j+1's bounds and asks L2 for those postings, which then arrive while
-        // the block scores job j.
+        // j+1's bounds. (Asking L2 for job j+1's postings at that point was
+        // measured: it cost more issue slots than the latency it hid.)
         Job jb = first_job(T.win, a.nlen, tile);
         uint32_t pf_hi[kPf], ps_lo[kPf];
         // the bucket and the intensity of this thread's lists tid + m * nthr
@@ -819,7 +808,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 }
             }
             if (!WIDE && (__reduce_or_sync(0xFFFFFFFFu, ovf) & 0x80000000u) && lane == 0) T.overflow = 1;
-            // ---- the next job's list bounds, and its postings into L2 ----
+            // ---- the next job's list bounds ----
             if (nj.l != kNoJob)
             {
                 const bool inter = !WIDE && job_interior(nj, dn.n);
@@ -827,16 +816,16 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 for (int m = 0; m < kPf; m++)
                 {
                     const uint32_t pr = tid + m * nthr;
-                    uint32_t cnt = 0;
+                    uint32_t cnt = 0, st = 0, en = 0;
                     if (pr < np)
                     {
-                        const uint32_t st = same ? lend[pr] : ps_lo[m], en = pf_hi[m];
+                        st = same ? lend[pr] : ps_lo[m];
+                        en = pf_hi[m];
                         if (inter && st < en) npass += en - st;
                         li_n[pr] = make_uint2(st, my_int[m]);
                         lend[pr] = en;
                         cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                         lo_n[pr] = cnt;
-                        prefetch_l2(dn.qp, st, en);
                     }
                     if (m * nthr + 32 * wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
                 }
@@ -844,18 +833,18 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 for (uint32_t base = kPf * nthr; base < np; base += (uint32_t)nthr)
                 {
                     const uint32_t pr = base + (uint32_t)tid;
-                    uint32_t cnt = 0;
+                    uint32_t cnt = 0, st = 0, en = 0;
                     if (pr < np)
                     {
                         const uint32_t k = pr / nbin, j = pr - k * nbin;
                         const uint32_t *col = dn.rows + (size_t)(pmoz[k] - a.dF + j) * dn.stride;
-                        const uint32_t st = same ? lend[pr] : row_lo(col, nj.c0), en = row_hi(col, nj.c1);
+                        st = same ? lend[pr] : row_lo(col, nj.c0);
+                        en = row_hi(col, nj.c1);
                         if (inter && st < en) npass += en - st;
                         li_n[pr] = make_uint2(st, pint[k]);
                         lend[pr] = en;
                         cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                         lo_n[pr] = cnt;
-                        prefetch_l2(dn.qp, st, en);
                     }
                     if (base + 32 * (uint32_t)wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
                 }
