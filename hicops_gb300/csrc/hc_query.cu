@@ -147,6 +147,7 @@ struct SmemTail
     unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations
     int2 win[HC_MAX_LENGTHS];  // the spectrum's window per length
     float lgf[kLgTable];
+    uint32_t wtail[32];        // per warp: candidates appended to its ring so far (this job)
     uint32_t gtc[kMaxGroups];  // per group of 32 lists of the next job: chunks
     uint32_t gtz[kMaxGroups];  // ... and non-empty lists
     LenS len[HC_MAX_LENGTHS];
@@ -871,6 +872,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             {
                 const uint4 *c4 = reinterpret_cast<const uint4 *>(card);
                 uint32_t qh = 0, qhead = 0;  // ring fill and head (warp-uniform)
+                if (lane == 0) T.wtail[wid] = 0;
+                __syncwarp();
                 auto pop_score = [&](uint32_t cnt) {
                     __syncwarp();
                     if ((uint32_t)lane < cnt)
@@ -927,20 +930,14 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t sw = bw + yw;
                     uint32_t m = thr7 ? (((sw | 0x80808080u) - thr4) | sw) & 0x80808080u
                                       : (__vcmpgeu4(sw, thr4) & 0x01010101u) << 7;
-                    // this lane's place in the warp's ring: an inclusive scan of the counts
+                    // this lane's place in the warp's ring: from the warp's
+                    // append counter (T.wtail = qhead + qh; lanes in any order)
                     const uint32_t n4 = __popc(m);
-                    uint32_t inc = n4;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1)
-                    {
-                        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                        if (lane >= o) inc += t;
-                    }
-                    const uint32_t tot = __shfl_sync(0xFFFFFFFFu, inc, 31);
+                    const uint32_t tot = __reduce_add_sync(0xFFFFFFFFu, n4);
                     if (tot == 0) continue;
                     if (qh + tot <= kWQ)
                     {
-                        uint32_t r = qhead + qh + inc - n4;
+                        uint32_t r = n4 ? atomicAdd(&T.wtail[wid], n4) : 0u;
                         while (m)
                         {
                             const int k = (__ffs(m) - 1) >> 3;
@@ -961,6 +958,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         // the ring would overflow: the two halves one after the other
                         push(wa, ca);
                         push(wb, cb);
+                        __syncwarp();
+                        if (lane == 0) T.wtail[wid] = qhead + qh;
+                        __syncwarp();
                     }
                 }
                 if (qh) pop_score(qh);
