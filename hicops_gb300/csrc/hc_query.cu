@@ -45,6 +45,7 @@ constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
 constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
+constexpr uint32_t kScanSlack = 128;   // scorecard slots past the tile (see smem_layout)
 
 struct SearchArgs
 {
@@ -174,7 +175,9 @@ __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bo
 {
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
-    o.qual = (size_t)tile * 8 * (wide ? 2 : 1);
+    // packed words: kScanSlack zero slots past the tile, so the scan reads
+    // and clears whole 128-candidate steps without bounds checks
+    o.qual = wide ? (size_t)tile * 16 : ((size_t)tile + kScanSlack) * 8;
     o.defer = o.qual;
     o.maxpairs = (uint32_t)maxpairs;
     o.loffs = (uint32_t)maxpairs + 4;
@@ -441,7 +444,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         const LenDev &ld = a.lens[l];
         T.len[l] = LenS{ld.qp, ld.rows, ld.stride, ld.n};
     }
-    for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
+    for (uint32_t i = tid; i < (tile + (WIDE ? 0u : kScanSlack)) * NW; i += nthr) card[i] = 0;
     if (tid == 0)
     {
         for (int k = 0; k < kPhases; k++) T.ph[k] = 0;
@@ -912,10 +915,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 const bool thr7 = a.thr <= 127u;
                 for (uint32_t base = first; base < ntile; base += step)
                 {
-                    // words past ntile are zero (the tile is cleared after use)
+                    // words past ntile are zero (the tile is cleared after use,
+                    // and the kScanSlack slots past the tile are never written)
                     const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
-                    const uint4 wa = ca < ntile ? c4[ca >> 1] : make_uint4(0u, 0u, 0u, 0u);
-                    const uint4 wb = cb < ntile ? c4[cb >> 1] : make_uint4(0u, 0u, 0u, 0u);
+                    const uint4 wa = c4[ca >> 1];
+                    const uint4 wb = c4[cb >> 1];
                     // the four candidates' counts (the top bytes of their b and y
                     // words) summed and compared as bytes: candidates ca, ca + 1,
                     // cb, cb + 1 in bytes 0..3 (each count < 128, so no carry)
@@ -969,8 +973,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 for (uint32_t base = first; base < ntile; base += step)
                 {
                     const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
-                    if (ca < ntile) z4[ca >> 1] = make_uint4(0u, 0u, 0u, 0u);
-                    if (cb < ntile) z4[cb >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                    z4[ca >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                    z4[cb >> 1] = make_uint4(0u, 0u, 0u, 0u);
                 }
             }
             else
