@@ -717,6 +717,18 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 // set one bit each at their first lane, and a lane's list is the
                 // one before plus the bits at or below it
                 uint32_t k0 = find_list(co, ncl, q0, lane);
+                if (co[k0 + 1u] >= q0 + 32u * G)  // warp-uniform: the whole grab lies in list k0
+                {
+                    const uint2 li = li_c[cl[k0]];
+                    const uint32_t p0 = (li.x & ~3u) + 4u * (q0 + (uint32_t)lane - co[k0]);
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+                    {
+                        inte[g] = li.y;
+                        v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + p0 + 128u * g));
+                    }
+                }
+                else
 #pragma unroll
                 for (int g = 0; g < G; g++)
                 {

@@ -491,16 +491,21 @@ void orc_tailfit(const double *yy, int cpsms, int hyp, int32_t *mu, int32_t *bet
                  int32_t *stt1_out, int32_t *end1_out, uint32_t *flags)
 {
     double mu_t = 0.0, beta_t = 4.0;
+    /* A top hyperscore past the histogram (flagged ORC_FLAG_HIST_OOB) makes
+     * the reference read survival[] beyond its 1002 bins (undefined): here,
+     * as on the device, bins past the histogram hold 0 and the slice stops
+     * at its last bin. */
     int end1 = hyp - 1;
-    for (int q = hyp - 1; q >= 0; q--)
+    for (int q = (hyp - 1 < ORC_HIST_BINS - 1 ? hyp - 1 : ORC_HIST_BINS - 1); q >= 0; q--)
         if (yy[q] >= 1.0) { end1 = q; break; }
     int stt1 = 0;
-    for (int q = 0; q <= end1; q++)
+    for (int q = 0; q <= end1 && q < ORC_HIST_BINS; q++)
         if (yy[q] >= 1.0) { stt1 = q; break; }
     if (stt1 == end1)
         end1 += 1;
     int n = end1 - stt1 + 1;
     if (n < 0) n = 0;
+    if (stt1 + n > ORC_HIST_BINS) n = ORC_HIST_BINS - stt1;
     if (cpsms < 1)
     {
         mu_t = 0;
