@@ -34,6 +34,9 @@ void free_len(LenHost &lh)
     cudaFree(lh.d_qA);
     cudaFree(lh.d_qp);
     cudaFree(lh.d_qion);
+    cudaFree(lh.d_qAs);
+    cudaFree(lh.d_qps);
+    cudaFree(lh.d_cls);
     cudaFree(lh.d_rows);
     const uint32_t L = lh.L;
     lh = LenHost();
@@ -115,6 +118,7 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
         return HC_ERR_CUDA;
     }
     make_ion_tables(ctx->p, &ctx->tables);
+    ctx->class_of.assign(kCodes, (uint8_t)kClassNone);
     QueryConst qc;
     make_query_const(&qc);
     {
@@ -158,6 +162,8 @@ int hc_ctx_destroy(hc_ctx *ctx)
     for (auto &lh : ctx->lens) free_len(lh);
     cudaFree(ctx->d_lens);
     cudaFree(ctx->d_tables);
+    cudaFree(ctx->d_classes);
+    cudaFree(ctx->d_class_of);
     cudaFree(ctx->d_qconst);
     cudaFree(ctx->qs.d_win);
     cudaFree(ctx->qs.d_wide);

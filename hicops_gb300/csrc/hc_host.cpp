@@ -162,6 +162,29 @@ void make_ion_tables(const hc_params &p, IonTables *t)
     t->max_mass = p.max_mass;
 }
 
+// The y1 keys, charges 0 .. maxz-1, of the entries with entry-class code
+// `code` (hc_index.cu, entry_code): the first y ion of k_ion_keys's loop,
+// i.e. utils.cpp:257-270 without mods and utils.cpp:441-500 with them (the
+// undivided sum plus the mod at the last residue, then integer division by
+// the charge); illegal masses give zero keys.
+void class_keys_of(const hc_params &p, const IonTables &t, uint32_t code, uint32_t *keys)
+{
+    const uint32_t top = p.max_mass * p.scale;
+    const bool illegal = code == kCodes - 1;
+    for (uint32_t z = 0; z < p.maxz && z < (uint32_t)kMaxZ; z++)
+    {
+        uint32_t v;
+        if (illegal) v = 0;
+        else if (!(code & 0x200u)) v = code < 26 ? t.yf[code][z] : 0u;
+        else
+        {
+            const uint32_t r = (code >> 4) & 0x1Fu, qy = code & 0xFu;
+            v = r < 26 ? (t.yfm[r][z] + (qy ? t.mod_mass[qy - 1] : 0u)) / (z + 1) : 0u;
+        }
+        keys[z] = (!illegal && v >= top) ? top - 1 : v;
+    }
+}
+
 void make_query_const(QueryConst *q)
 {
     // hcp::utils::lgfact (utils.h:115-131): val[0] = val[1] = log10(1),

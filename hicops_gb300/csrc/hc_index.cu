@@ -540,6 +540,139 @@ __global__ void k_qpost_ids(const uint32_t *__restrict__ bA, const uint32_t *__r
     }
 }
 
+// ---- entry classes and the search postings ------------------------------------
+// (see ClassKeys in hc_internal.h)
+
+// The class code of one entry: the facts k_ion_keys reads for the first y
+// ion (legal mass, mod path, last residue, the mod there); kCodes - 1 for an
+// illegal mass, and for a residue byte outside 'A'..'Z' a code no entry's
+// postings can match (the build check then leaves it unclassed).
+__device__ __forceinline__ uint32_t entry_code(double minm, double maxm, uint32_t L, const uint8_t *seq, double m,
+                                               uint32_t mn, uint64_t st)
+{
+    bool legal = (m >= minm && m <= maxm);
+    if (mn != 0 && legal && !(m > minm && m < maxm)) legal = false;
+    if (!legal) return kCodes - 1;
+    const uint32_t rl = (uint32_t)seq[L - 1] - 'A';
+    if (rl >= 26u) return kCodes - 2;
+    if (mn == 0) return rl;
+    // the last mod, when the last residue carries one (utils.cpp:480-500)
+    uint32_t last = 0;
+    for (int i = 0; i < 8; i++)
+    {
+        const uint32_t q = (mn >> (4 * i)) & 0xFu;
+        if (q) last = q;
+    }
+    const uint32_t qy = ((st >> (L - 1)) & 1ull) ? last : 0u;
+    return 0x200u | (rl << 4) | qy;
+}
+
+__global__ void k_entry_codes(double minm, double maxm, uint32_t L, uint32_t n, const float *__restrict__ mass,
+                              const uint32_t *__restrict__ seqid, const uint64_t *__restrict__ sites,
+                              const uint32_t *__restrict__ modnum, const uint8_t *__restrict__ seqs,
+                              uint16_t *__restrict__ code, uint8_t *__restrict__ used)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t c = entry_code(minm, maxm, L, seqs + (size_t)seqid[k] * L, (double)mass[k], modnum[k], sites[k]);
+    code[k] = (uint16_t)c;
+    used[c] = 1;
+}
+
+__global__ void k_entry_classes(const uint16_t *__restrict__ code, uint32_t n, const uint8_t *__restrict__ class_of,
+                                uint8_t *__restrict__ cls)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    cls[k] = class_of[code[k]];
+}
+
+// the charge of a query posting's ion when it is a y1 ion, else -1;
+// ion = series * half + charge * (L - 1) + position
+__device__ __forceinline__ int y1_charge(uint32_t ion, uint32_t Lm1, uint32_t half)
+{
+    if (ion < half || (ion - half) % Lm1) return -1;
+    return (int)((ion - half) / Lm1);
+}
+
+// One warp per bucket: every y1 posting of a classed entry must lie in its
+// class's key bucket; bad[e] = 1 marks the entries where one does not (they
+// lose their class).
+__global__ void k_class_check(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
+                              const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
+                              const uint8_t *__restrict__ cls, const ClassKeys *__restrict__ ck,
+                              uint8_t *__restrict__ bad)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
+    {
+        const uint32_t e1 = qA[b + 1];
+        for (uint32_t i = qA[b] + lane; i < e1; i += 32)
+        {
+            const uint32_t x = qp[i];
+            if (x == kQpostPad) continue;
+            const int z = y1_charge(qion[i], Lm1, half);
+            if (z < 0) continue;
+            const uint32_t e = x >> kQpEntryShift, c = cls[e];
+            if (c != kClassNone && ck->key[c][z] != b) bad[e] = 1;
+        }
+    }
+}
+
+__global__ void k_class_fix(uint8_t *__restrict__ cls, const uint8_t *__restrict__ bad, uint32_t n)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && bad[k]) cls[k] = (uint8_t)kClassNone;
+}
+
+// a query posting stays in the search postings unless it is padding or the
+// y1 posting of a classed entry
+__device__ __forceinline__ bool search_kept(uint32_t x, uint32_t ion, uint32_t Lm1, uint32_t half,
+                                            const uint8_t *__restrict__ cls)
+{
+    if (x == kQpostPad) return false;
+    return y1_charge(ion, Lm1, half) < 0 || cls[x >> kQpEntryShift] == kClassNone;
+}
+
+// One warp per bucket: the padded size of its search postings.
+__global__ void k_search_counts(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
+                                const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
+                                const uint8_t *__restrict__ cls, uint32_t *__restrict__ qAs)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
+    {
+        uint32_t c = 0;
+        const uint32_t e1 = qA[b + 1];
+        for (uint32_t i = qA[b] + lane; i < e1; i += 32) c += search_kept(qp[i], qion[i], Lm1, half, cls) ? 1u : 0u;
+        c = __reduce_add_sync(0xFFFFFFFFu, c);
+        if (lane == 0) qAs[b] = (c + 3u) & ~3u;
+    }
+}
+
+// One warp per bucket: its search postings, in order, at qAs[b].
+__global__ void k_search_scatter(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
+                                 const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
+                                 const uint8_t *__restrict__ cls, const uint32_t *__restrict__ qAs,
+                                 uint32_t *__restrict__ qps)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
+    {
+        uint32_t o = qAs[b];
+        const uint32_t e1 = qA[b + 1];
+        for (uint32_t base = qA[b]; base < e1; base += 32)
+        {
+            const uint32_t i = base + lane;
+            const uint32_t x = i < e1 ? qp[i] : kQpostPad;
+            const bool k = i < e1 && search_kept(x, qion[i], Lm1, half, cls);
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, k);
+            if (k) qps[o + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = x;
+            o += (uint32_t)__popc(bal);
+        }
+    }
+}
+
 template <class T>
 cudaError_t dalloc(T **p, size_t n)
 {
@@ -781,19 +914,102 @@ int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids)
     return build_rows(ctx, lh);
 }
 
-// The row table of a length from its query postings (qA, qp, n set).
+// Classes for the codes seen in `used` that have none yet (ids are only ever
+// added, so the lengths built before keep theirs), and the device copies.
+static int add_classes(hc_ctx *ctx, const std::vector<uint8_t> &used)
+{
+    bool changed = false;
+    for (uint32_t code = 0; code < kCodes; code++)
+    {
+        if (!used[code] || code == kCodes - 2 || ctx->class_of[code] != kClassNone || ctx->classes.n >= kMaxClasses)
+            continue;
+        const uint32_t id = ctx->classes.n++;
+        ctx->class_of[code] = (uint8_t)id;
+        class_keys_of(ctx->p, ctx->tables, code, ctx->classes.key[id]);
+        for (uint32_t z = 0; z < ctx->p.maxz; z++)
+            ctx->classes.maxkey = std::max(ctx->classes.maxkey, ctx->classes.key[id][z]);
+        changed = true;
+    }
+    if (!ctx->d_classes)
+    {
+        HC_CUDA(ctx, cudaMalloc((void **)&ctx->d_classes, sizeof(ClassKeys)));
+        HC_CUDA(ctx, cudaMalloc((void **)&ctx->d_class_of, kCodes));
+        changed = true;
+    }
+    if (changed)
+    {
+        HC_CUDA(ctx, cudaMemcpy(ctx->d_classes, &ctx->classes, sizeof(ClassKeys), cudaMemcpyHostToDevice));
+        HC_CUDA(ctx, cudaMemcpy(ctx->d_class_of, ctx->class_of.data(), kCodes, cudaMemcpyHostToDevice));
+    }
+    return HC_SUCCESS;
+}
+
+// The search side of a length from its query postings (qA, qp, qion and the
+// entries set): each entry's class (checked against its own y1 postings),
+// the search postings (the query postings less the y1 postings of classed
+// entries, buckets padded to 4 words) and their row table.
 int build_rows(hc_ctx *ctx, LenHost &lh)
 {
-    const uint32_t nb = ctx->p.max_mass * ctx->p.scale;
+    cudaStream_t st = ctx->stream;
+    const uint32_t nb = ctx->p.max_mass * ctx->p.scale, n = lh.n, Lm1 = lh.L - 1;
+    const uint32_t half = ctx->p.maxz * Lm1;
     cudaFree(lh.d_rows);
-    lh.d_rows = nullptr;
-    lh.stride = (lh.n + kRowG - 1) / kRowG + 1;
+    cudaFree(lh.d_qAs);
+    cudaFree(lh.d_qps);
+    cudaFree(lh.d_cls);
+    lh.d_rows = lh.d_qAs = lh.d_qps = nullptr;
+    lh.d_cls = nullptr;
+    HC_CUDA(ctx, dalloc(&lh.d_cls, (size_t)n + 4));  // +4: the search reads class bytes in fours
+    HC_CUDA(ctx, dalloc(&lh.d_qAs, (size_t)nb + 1));
+    HC_CUDA(ctx, cudaMemsetAsync(lh.d_cls, (int)kClassNone, (size_t)n + 4, st));
+    const unsigned eblocks = (n + 255) / 256;
+    const unsigned wblocks = (unsigned)std::min<uint64_t>((nb + 7) / 8, (uint64_t)ctx->sm_count * 64);
+    Scratch scr;
+    if (n > 0)
+    {
+        uint16_t *code;
+        uint8_t *used, *bad;
+        HC_CUDA(ctx, scr.alloc(&code, n));
+        HC_CUDA(ctx, scr.alloc(&used, (size_t)kCodes));
+        HC_CUDA(ctx, scr.alloc(&bad, (size_t)n));
+        HC_CUDA(ctx, cudaMemsetAsync(used, 0, kCodes, st));
+        HC_CUDA(ctx, cudaMemsetAsync(bad, 0, n, st));
+        k_entry_codes<<<eblocks, 256, 0, st>>>((double)ctx->p.min_mass, (double)ctx->p.max_mass, lh.L, n, lh.d_mass,
+                                              lh.d_seqid, lh.d_sites, lh.d_modnum, lh.d_seqs, code, used);
+        HC_CUDA(ctx, cudaGetLastError());
+        std::vector<uint8_t> hused(kCodes);
+        HC_CUDA(ctx, cudaMemcpyAsync(hused.data(), used, kCodes, cudaMemcpyDeviceToHost, st));
+        HC_CUDA(ctx, cudaStreamSynchronize(st));
+        const int rc = add_classes(ctx, hused);
+        if (rc) return rc;
+        k_entry_classes<<<eblocks, 256, 0, st>>>(code, n, ctx->d_class_of, lh.d_cls);
+        k_class_check<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, ctx->d_classes,
+                                               bad);
+        k_class_fix<<<eblocks, 256, 0, st>>>(lh.d_cls, bad, n);
+        HC_CUDA(ctx, cudaGetLastError());
+    }
+    uint32_t *stmp = nullptr;
+    HC_CUDA(ctx, scr.alloc(&stmp, scan_tmp_words((size_t)nb + 1)));
+    HC_CUDA(ctx, cudaMemsetAsync(lh.d_qAs + nb, 0, 4, st));
+    k_search_counts<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, lh.d_qAs);
+    HC_CUDA(ctx, cudaGetLastError());
+    HC_CUDA(ctx, scan_exclusive(lh.d_qAs, (size_t)nb + 1, stmp, st));
+    uint32_t total = 0;
+    HC_CUDA(ctx, cudaMemcpyAsync(&total, lh.d_qAs + nb, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    lh.nsearch = total;
+    HC_CUDA(ctx, dalloc(&lh.d_qps, (size_t)total + kIaPad));
+    HC_CUDA(ctx, cudaMemsetAsync(lh.d_qps, 0xFF, 4 * ((size_t)total + kIaPad), st));
+    k_search_scatter<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, lh.d_qAs,
+                                              lh.d_qps);
+    HC_CUDA(ctx, cudaGetLastError());
+    lh.stride = (n + kRowG - 1) / kRowG + 1;
     HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
     const uint64_t rt = (uint64_t)nb * lh.stride;
     const unsigned blocks = (unsigned)std::min<uint64_t>((rt + 255) / 256, (uint64_t)ctx->sm_count * 64);
-    k_row_table<<<blocks, 256, 0, ctx->stream>>>(lh.d_qA, lh.d_qp, nb, lh.stride, lh.n, lh.d_rows);
+    k_row_table<<<blocks, 256, 0, st>>>(lh.d_qAs, lh.d_qps, nb, lh.stride, n, lh.d_rows);
     HC_CUDA(ctx, cudaGetLastError());
-    HC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
     return HC_SUCCESS;
 }
 

@@ -33,6 +33,33 @@ constexpr uint32_t kQpostPad = 0xFFFFFFFFu;
 constexpr uint32_t kQpEntryShift = 3;
 constexpr uint32_t kQpMaxEntries = (1u << 29) - 2;  // entries of one length the encoding holds
 
+// Entry classes. An entry's first y ion (y1), at every fragment charge, is
+// fixed by a few facts about the entry: whether its mass is legal, whether it
+// takes the mod-spectrum path (utils.cpp:378-505 when it carries mods), its
+// last residue and the mod there. Those facts form a small "code"; entries
+// with the same code share their y1 keys (a tryptic database has a few dozen
+// codes, and y1 postings are about half of all the postings a search
+// visits). Every code seen gets a class id with the class's keys; the search
+// postings leave out the y1 postings of classed entries, and the search
+// starts each candidate's y word with what its class's keys collect from the
+// spectrum's peaks (the same count and intensity sum the left-out postings
+// would have added). The index build checks every left-out posting against
+// its class's key, so the code only has to be right for an entry to be
+// classed, never for the results to be right. (The first b ion has as few
+// codes, but its postings are a tenth of the total: classing it costs the
+// search more per candidate than its postings do.)
+constexpr uint32_t kMaxClasses = 127;   // class ids 0 .. 126
+constexpr uint32_t kClassNone = 127;    // an entry without a class (adds nothing)
+constexpr uint32_t kCodes = 1u << 10;   // codes: legal, path, last residue, mod at the last residue
+
+// The class keys, per class and charge.
+struct ClassKeys
+{
+    uint32_t n;         // classes
+    uint32_t maxkey;    // the largest key of any class (peaks above it + dF cannot reach one)
+    uint32_t key[kMaxClasses][kMaxZ];
+};
+
 // One peptide length's device-resident index. All arrays are device pointers.
 struct LenDev
 {
@@ -48,7 +75,9 @@ struct LenDev
     const uint32_t *bA;
     const uint32_t *qA;            // bucket starts in qp (multiples of 4)
     const uint32_t *qp;            // query postings (see kQpostPad)
-    const uint32_t *rows;          // row table over qp, [bucket][k] with `stride` entries per bucket
+    const uint32_t *qps;           // search postings: qp without the y1 postings of classed entries
+    const uint32_t *rows;          // row table over qps, [bucket][k] with `stride` entries per bucket
+    const uint8_t *cls;            // per entry: its class (kClassNone: none)
 };
 
 // Integer ion-key tables, derived on the host with the reference's double
@@ -88,7 +117,11 @@ struct LenHost
     uint32_t *d_qA = nullptr;    // padded bucket starts (max_mass*scale + 1)
     uint32_t *d_qp = nullptr;    // query postings, qA[nb] words (+ kIaPad)
     uint16_t *d_qion = nullptr;  // ion of each query posting (same positions as d_qp)
-    uint32_t *d_rows = nullptr;  // row table (max_mass*scale buckets x stride)
+    uint32_t *d_qAs = nullptr;   // search postings: bucket starts (multiples of 4)
+    uint32_t *d_qps = nullptr;   // search postings (query postings less the classed y1 ones)
+    uint8_t *d_cls = nullptr;    // per entry: its class
+    uint64_t nsearch = 0;        // search postings (without padding)
+    uint32_t *d_rows = nullptr;  // row table over the search postings (max_mass*scale buckets x stride)
     uint32_t stride = 0;
     bool built = false;
 };
@@ -160,6 +193,11 @@ struct hc_ctx
     hc::LenDev *d_lens = nullptr;
     hc::IonTables tables{};
     hc::IonTables *d_tables = nullptr;
+    // entry classes (shared by all lengths; ids are only ever added)
+    std::vector<uint8_t> class_of;     // code -> class id
+    hc::ClassKeys classes{};
+    hc::ClassKeys *d_classes = nullptr;
+    uint8_t *d_class_of = nullptr;
     hc::QueryConst *d_qconst = nullptr;
     hc::QueryScratch qs;
     std::string last_error;
@@ -212,7 +250,8 @@ void division_magic(uint32_t d, uint32_t *magic, uint32_t *sh);
 // hc_index.cu
 int build_length_device(hc_ctx *ctx, LenHost &lh, const hc_entry *h_entries, bool sort_by_mass);
 int build_query_postings(hc_ctx *ctx, LenHost &lh, const uint32_t *d_ids);
-int build_rows(hc_ctx *ctx, LenHost &lh);
+int build_rows(hc_ctx *ctx, LenHost &lh);  // entry classes, search postings and their row table
+void class_keys_of(const hc_params &p, const IonTables &t, uint32_t code, uint32_t *keys);
 int check_query_postings(hc_ctx *ctx, const LenHost &lh, uint64_t qtotal);
 void free_len(LenHost &lh);
 int export_ids(hc_ctx *ctx, const LenHost &lh, uint32_t *d_ids);

@@ -67,6 +67,8 @@ struct SearchArgs
     const uint32_t *nonly_dev;  // its length, in device memory
     const uint32_t *order;  // optional processing order (longest first)
     uint32_t persistent;    // 1: CTAs loop over a work counter; 0: one spectrum per CTA
+    uint32_t maxz;
+    const ClassKeys *classes;   // entry classes (null: none built)
     unsigned long long *phase;  // optional: SM cycles per phase, summed over CTAs (kPhases)
 };
 
@@ -117,8 +119,9 @@ struct Card<true>
 // the kernel's lifetime (one global read per CTA instead of one per job).
 struct LenS
 {
-    const uint32_t *qp, *rows;
+    const uint32_t *qp, *rows;  // search postings and their row table
     uint32_t stride, n;
+    const uint8_t *cls;         // entry classes (4 bytes of padding past the last entry)
 };
 
 constexpr uint32_t kMaxDF = 16;  // the largest dF hc_ctx_create accepts
@@ -152,6 +155,13 @@ struct SmemTail
     uint32_t gtc[kMaxGroups];  // per group of 32 lists of the next job: chunks
     uint32_t gtz[kMaxGroups];  // ... and non-empty lists
     LenS len[HC_MAX_LENGTHS];
+    // per entry class: what its y1 keys collect from the spectrum's valid
+    // peaks, as a wide word [count:24 | sum:40] and packed [count:8 |
+    // sum:24]; entry kClassNone stays zero
+    unsigned long long ucls[kMaxClasses + 1];
+    uint32_t upk[kMaxClasses + 1];
+    uint32_t low[HC_QALEN];    // valid peaks that can reach a class key
+    uint32_t nlow;
 };
 
 // adds the cycles since the last mark to phase k (thread 0 only, after a barrier)
@@ -442,7 +452,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     for (uint32_t l = tid; l < a.nlen; l += nthr)
     {
         const LenDev &ld = a.lens[l];
-        T.len[l] = LenS{ld.qp, ld.rows, ld.stride, ld.n};
+        T.len[l] = LenS{ld.qps, ld.rows, ld.stride, ld.n, ld.cls};
     }
     for (uint32_t i = tid; i < (tile + (WIDE ? 0u : kScanSlack)) * NW; i += nthr) card[i] = 0;
     if (tid == 0)
@@ -549,11 +559,14 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             T.overflow = 0;
             T.bytes = 0;
             T.nv = 0;
+            T.nlow = 0;
         }
         for (uint32_t l = tid; l < a.nlen; l += nthr) T.win[l] = a.win[(size_t)s * a.nlen + l];
+        for (uint32_t i = tid; i < kMaxClasses + 1; i += nthr) T.ucls[i] = 0ull;
         __syncthreads();
         // valid peaks (dslim_query.cpp:625): dF < qion < max*scale - 1 - dF
         {
+            const uint32_t lowlim = a.classes ? __ldg(&a.classes->maxkey) + a.dF : 0u;
             const uint32_t p0 = a.idx[s], p1 = a.idx[s + 1];
             for (uint32_t k = p0 + tid; k < p1; k += nthr)
             {
@@ -567,6 +580,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         pmoz[slot] = q;
                         pint[slot] = a.inten[k];
+                        if (q <= lowlim) T.low[atomicAdd(&T.nlow, 1u)] = slot;
                     }
                 }
             }
@@ -594,6 +608,34 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             close = __syncthreads_or(close);
             if (tid == 0) T.noret = (!close && a.lens[a.nlen - 1].half < 128u) ? 1u : 0u;
         }
+        // the class adds: for each class, charge and valid peak whose bins
+        // (q - dF .. q + dF) hold the class's y1 key, what the left-out
+        // posting of every entry of the class would add there
+        if (a.classes)
+        {
+            const uint32_t nz = a.maxz, tot = a.classes->n * nz, nlow = T.nlow;
+            for (uint32_t i = tid; i < tot; i += nthr)
+            {
+                const uint32_t c = i / nz, z = i - c * nz;
+                const uint32_t key = a.classes->key[c][z];
+                unsigned long long acc = 0;
+                for (uint32_t t = 0; t < nlow; t++)
+                {
+                    const uint32_t sl = T.low[t], q = pmoz[sl];
+                    if (q <= key + a.dF && q + a.dF >= key) acc += (1ull << 40) | pint[sl];
+                }
+                if (acc) atomicAdd(&T.ucls[c], acc);
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < kMaxClasses + 1; i += nthr)
+        {
+            // packed: a count of 64 or more from a class alone is redone wide
+            const unsigned long long u = T.ucls[i];
+            if (!WIDE && (u >> 40) >= 64u) T.overflow = 1;
+            T.upk[i] = ((uint32_t)(u >> 40) << 24) | (uint32_t)(u & 0xFFFFFFull);
+        }
+        __syncthreads();
         const uint32_t np = nv * nbin;
         my_best = 0;
         my_shp = 0;
@@ -650,6 +692,27 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     loff[pr] = cnt;
                 }
                 if (base + 32 * (uint32_t)wid < np) group_totals(cnt, (pr >> 5), lane, T.gtc, T.gtz);
+            }
+            // the first job's scorecard: each candidate's y word starts with its class's adds
+            {
+                const uint32_t nt0 = jb.c1 - jb.c0;
+                const uint8_t *cl0 = d.cls + jb.c0;
+                for (uint32_t c = tid; c < nt0; c += nthr)
+                {
+                    const uint32_t k = __ldg(cl0 + c);
+                    if constexpr (!WIDE)
+                    {
+                        const uint32_t wy = T.upk[k];
+                        card[2 * c + 1] = wy;
+                        npass += wy >> 24;
+                    }
+                    else
+                    {
+                        const W wy = T.ucls[k];
+                        card[2 * c + 1] = wy;
+                        npass += (uint32_t)(wy >> 40);
+                    }
+                }
             }
             __syncthreads();
             for (uint32_t g = nw - 1 - (uint32_t)wid; g < ng; g += nw)
@@ -980,26 +1043,63 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                 }
                 if (qh) pop_score(qh);
-                // the warp's own words, now read: clear them for the next job
+                // the next job's candidates and their classes (its scorecard start)
+                const uint32_t nn = nj.l != kNoJob ? nj.c1 - nj.c0 : 0u;
+                const uint8_t *ncls = nn ? T.len[nj.l].cls + nj.c0 : nullptr;
+                // the warp's own words, now read: the next job's start there,
+                // four consecutive candidates per lane (b word zero, y word
+                // its class's adds; zero past the next job's end)
                 uint4 *z4 = reinterpret_cast<uint4 *>(card);
-                for (uint32_t base = first; base < ntile; base += step)
+                const uint32_t lim = max(ntile, nn);
+                const bool al4 = (nj.c0 & 3u) == 0u;  // class bytes readable as one word (warp-uniform)
+                for (uint32_t base = first; base < lim; base += step)
                 {
-                    const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
-                    z4[ca >> 1] = make_uint4(0u, 0u, 0u, 0u);
-                    z4[cb >> 1] = make_uint4(0u, 0u, 0u, 0u);
+                    const uint32_t c = base + 4 * (uint32_t)lane;
+                    uint32_t k4 = kClassNone * 0x01010101u;
+                    if (c < nn)
+                    {
+                        if (al4) k4 = __ldg(reinterpret_cast<const uint32_t *>(ncls + c));
+                        else
+                            k4 = (uint32_t)__ldg(ncls + c) | ((uint32_t)__ldg(ncls + c + 1) << 8) |
+                                 ((uint32_t)__ldg(ncls + c + 2) << 16) | ((uint32_t)__ldg(ncls + c + 3) << 24);
+                        if (c + 4 > nn)
+                        {
+                            const uint32_t keep = (1u << (8 * (nn - c))) - 1u;  // bytes of candidates < nn
+                            k4 = (k4 & keep) | (kClassNone * 0x01010101u & ~keep);
+                        }
+                    }
+                    const uint32_t y0 = T.upk[k4 & 0xFFu], y1 = T.upk[(k4 >> 8) & 0xFFu];
+                    const uint32_t y2 = T.upk[(k4 >> 16) & 0xFFu], y3 = T.upk[k4 >> 24];
+                    z4[c >> 1] = make_uint4(0u, y0, 0u, y1);
+                    z4[(c >> 1) + 1] = make_uint4(0u, y2, 0u, y3);
+                    npass += (y0 >> 24) + (y1 >> 24) + (y2 >> 24) + (y3 >> 24);
                 }
             }
             else
             {
-                // wide words: one candidate per thread, every one checked, then cleared
-                for (uint32_t c = tid; c < ntile; c += nthr)
+                // wide words: one candidate per thread, every one checked, then
+                // set to the next job's start (y word: class adds; zero past its end)
+                const uint32_t nn = nj.l != kNoJob ? nj.c1 - nj.c0 : 0u;
+                const uint8_t *ncls = nn ? T.len[nj.l].cls + nj.c0 : nullptr;
+                const uint32_t lim = max(ntile, nn);
+                for (uint32_t c = tid; c < lim; c += nthr)
                 {
-                    uint32_t bc, yc, shp;
-                    uint64_t ib, iy;
-                    decode<WIDE>(card, c, bc, yc, shp, ib, iy);
-                    if (shp >= a.min_shp && shp != 0) score_one(bc, yc, ib, iy, shp, ~(key_l | ((c0 + c) & 0xFFFFFF)));
+                    if (c < ntile)
+                    {
+                        uint32_t bc, yc, shp;
+                        uint64_t ib, iy;
+                        decode<WIDE>(card, c, bc, yc, shp, ib, iy);
+                        if (shp >= a.min_shp && shp != 0)
+                            score_one(bc, yc, ib, iy, shp, ~(key_l | ((c0 + c) & 0xFFFFFF)));
+                    }
+                    W wy = 0;
+                    if (c < nn)
+                    {
+                        wy = T.ucls[__ldg(ncls + c)];
+                        npass += (uint32_t)(wy >> 40);
+                    }
                     card[2 * c] = 0;
-                    card[2 * c + 1] = 0;
+                    card[2 * c + 1] = wy;
                 }
             }
             {
@@ -1497,7 +1597,9 @@ static void fill_lendev(const hc_ctx *ctx, const LenHost &lh, LenDev &d)
     d.bA = lh.d_bA;
     d.qA = lh.d_qA;
     d.qp = lh.d_qp;
+    d.qps = lh.d_qps;
     d.rows = lh.d_rows;
+    d.cls = lh.d_cls;
 }
 
 int sync_lengths(hc_ctx *ctx)
@@ -1576,6 +1678,8 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.tile = ctx->tuning.tile;
     a.defer_cap = ctx->tuning.defer_cap;
     a.persistent = sched != 1;
+    a.maxz = ctx->p.maxz;
+    a.classes = ctx->d_classes;
     a.phase = ctx->d_phase;
     int launches = 4;
     if (sched == 2)
@@ -1729,6 +1833,8 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     a.defer_cap = ctx->tuning.defer_cap;
     const uint32_t sched = ctx->tuning.schedule;
     a.persistent = sched != 1;
+    a.maxz = ctx->p.maxz;
+    a.classes = ctx->d_classes;
     int launches = 4;
     if (sched == 2)
     {
