@@ -595,27 +595,45 @@ __device__ __forceinline__ int y1_charge(uint32_t ion, uint32_t Lm1, uint32_t ha
     return (int)((ion - half) / Lm1);
 }
 
-// One warp per bucket: every y1 posting of a classed entry must lie in its
-// class's key bucket; bad[e] = 1 marks the entries where one does not (they
-// lose their class).
+constexpr uint32_t kPosChunk = 64;  // postings per thread in the flat kernels below
+
+// The bucket holding position i of the query postings, from a bucket b with
+// qA[b] <= i: b itself while i is inside it, else the last bucket starting at
+// or before i (a binary search, so runs of empty buckets cost no walk).
+__device__ __forceinline__ uint32_t bucket_at(const uint32_t *__restrict__ qA, uint32_t nb, uint32_t i, uint32_t b)
+{
+    if (qA[b + 1] > i) return b;
+    uint32_t lo = b + 1, hi = nb;
+    while (lo < hi)
+    {
+        const uint32_t m = (lo + hi + 1) >> 1;
+        if (qA[m] <= i) lo = m;
+        else hi = m - 1;
+    }
+    return lo;
+}
+
+// kPosChunk postings per thread: every y1 posting of a classed entry must lie
+// in its class's key bucket; bad[e] = 1 marks the entries where one does not
+// (they lose their class).
 __global__ void k_class_check(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
-                              const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
-                              const uint8_t *__restrict__ cls, const ClassKeys *__restrict__ ck,
+                              const uint16_t *__restrict__ qion, uint32_t nb, uint32_t total, uint32_t Lm1,
+                              uint32_t half, const uint8_t *__restrict__ cls, const ClassKeys *__restrict__ ck,
                               uint8_t *__restrict__ bad)
 {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
+    const uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPosChunk;
+    if (i0 >= total) return;
+    const uint32_t i1 = (uint32_t)min((uint64_t)total, i0 + kPosChunk);
+    uint32_t b = bucket_at(qA, nb, (uint32_t)i0, 0);
+    for (uint32_t i = (uint32_t)i0; i < i1; i++)
     {
-        const uint32_t e1 = qA[b + 1];
-        for (uint32_t i = qA[b] + lane; i < e1; i += 32)
-        {
-            const uint32_t x = qp[i];
-            if (x == kQpostPad) continue;
-            const int z = y1_charge(qion[i], Lm1, half);
-            if (z < 0) continue;
-            const uint32_t e = x >> kQpEntryShift, c = cls[e];
-            if (c != kClassNone && ck->key[c][z] != b) bad[e] = 1;
-        }
+        const uint32_t x = qp[i];
+        if (x == kQpostPad) continue;
+        const int z = y1_charge(qion[i], Lm1, half);
+        if (z < 0) continue;
+        b = bucket_at(qA, nb, i, b);
+        const uint32_t e = x >> kQpEntryShift, c = cls[e];
+        if (c != kClassNone && ck->key[c][z] != b) bad[e] = 1;
     }
 }
 
@@ -634,42 +652,38 @@ __device__ __forceinline__ bool search_kept(uint32_t x, uint32_t ion, uint32_t L
     return y1_charge(ion, Lm1, half) < 0 || cls[x >> kQpEntryShift] == kClassNone;
 }
 
-// One warp per bucket: the padded size of its search postings.
-__global__ void k_search_counts(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
-                                const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
-                                const uint8_t *__restrict__ cls, uint32_t *__restrict__ qAs)
+// keep[i] = 1 for a query posting that stays in the search postings, else 0
+__global__ void k_search_keep(const uint32_t *__restrict__ qp, const uint16_t *__restrict__ qion, uint32_t total,
+                              uint32_t Lm1, uint32_t half, const uint8_t *__restrict__ cls, uint32_t *__restrict__ keep)
 {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
-    {
-        uint32_t c = 0;
-        const uint32_t e1 = qA[b + 1];
-        for (uint32_t i = qA[b] + lane; i < e1; i += 32) c += search_kept(qp[i], qion[i], Lm1, half, cls) ? 1u : 0u;
-        c = __reduce_add_sync(0xFFFFFFFFu, c);
-        if (lane == 0) qAs[b] = (c + 3u) & ~3u;
-    }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
+        keep[i] = search_kept(qp[i], qion[i], Lm1, half, cls) ? 1u : 0u;
 }
 
-// One warp per bucket: its search postings, in order, at qAs[b].
-__global__ void k_search_scatter(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
-                                 const uint16_t *__restrict__ qion, uint32_t nb, uint32_t Lm1, uint32_t half,
-                                 const uint8_t *__restrict__ cls, const uint32_t *__restrict__ qAs,
-                                 uint32_t *__restrict__ qps)
+// the padded size of each bucket's search postings, from the exclusive scan S
+// of the keep flags; entry nb is 0 (the scan makes it the total)
+__global__ void k_search_counts(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ S, uint32_t nb,
+                                uint32_t *__restrict__ qAs)
 {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += (gridDim.x * blockDim.x) >> 5)
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += gridDim.x * blockDim.x)
+        qAs[b] = b < nb ? ((S[qA[b + 1]] - S[qA[b]] + 3u) & ~3u) : 0u;
+}
+
+// kPosChunk postings per thread: each kept posting to its place, bucket b's
+// at qAs[b] in their order.
+__global__ void k_search_scatter(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
+                                 const uint32_t *__restrict__ S, uint32_t nb, uint32_t total,
+                                 const uint32_t *__restrict__ qAs, uint32_t *__restrict__ qps)
+{
+    const uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPosChunk;
+    if (i0 >= total) return;
+    const uint32_t i1 = (uint32_t)min((uint64_t)total, i0 + kPosChunk);
+    uint32_t b = bucket_at(qA, nb, (uint32_t)i0, 0);
+    for (uint32_t i = (uint32_t)i0; i < i1; i++)
     {
-        uint32_t o = qAs[b];
-        const uint32_t e1 = qA[b + 1];
-        for (uint32_t base = qA[b]; base < e1; base += 32)
-        {
-            const uint32_t i = base + lane;
-            const uint32_t x = i < e1 ? qp[i] : kQpostPad;
-            const bool k = i < e1 && search_kept(x, qion[i], Lm1, half, cls);
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, k);
-            if (k) qps[o + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = x;
-            o += (uint32_t)__popc(bal);
-        }
+        if (S[i + 1] == S[i]) continue;  // not kept
+        b = bucket_at(qA, nb, i, b);
+        qps[qAs[b] + S[i] - S[qA[b]]] = qp[i];
     }
 }
 
@@ -963,7 +977,10 @@ int build_rows(hc_ctx *ctx, LenHost &lh)
     HC_CUDA(ctx, dalloc(&lh.d_qAs, (size_t)nb + 1));
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_cls, (int)kClassNone, (size_t)n + 4, st));
     const unsigned eblocks = (n + 255) / 256;
-    const unsigned wblocks = (unsigned)std::min<uint64_t>((nb + 7) / 8, (uint64_t)ctx->sm_count * 64);
+    uint32_t qtotal = 0;  // query postings with padding
+    HC_CUDA(ctx, cudaMemcpyAsync(&qtotal, lh.d_qA + nb, 4, cudaMemcpyDeviceToHost, st));
+    HC_CUDA(ctx, cudaStreamSynchronize(st));
+    const unsigned pblocks = (unsigned)(((uint64_t)qtotal + 256ull * kPosChunk - 1) / (256ull * kPosChunk));
     Scratch scr;
     if (n > 0)
     {
@@ -983,25 +1000,37 @@ int build_rows(hc_ctx *ctx, LenHost &lh)
         const int rc = add_classes(ctx, hused);
         if (rc) return rc;
         k_entry_classes<<<eblocks, 256, 0, st>>>(code, n, ctx->d_class_of, lh.d_cls);
-        k_class_check<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, ctx->d_classes,
-                                               bad);
+        if (qtotal)
+            k_class_check<<<pblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, qtotal, Lm1, half, lh.d_cls,
+                                                   ctx->d_classes, bad);
         k_class_fix<<<eblocks, 256, 0, st>>>(lh.d_cls, bad, n);
         HC_CUDA(ctx, cudaGetLastError());
     }
-    uint32_t *stmp = nullptr;
-    HC_CUDA(ctx, scr.alloc(&stmp, scan_tmp_words((size_t)nb + 1)));
-    HC_CUDA(ctx, cudaMemsetAsync(lh.d_qAs + nb, 0, 4, st));
-    k_search_counts<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, lh.d_qAs);
+    // keep flags of the query postings, their exclusive scan S (S[qtotal] =
+    // postings kept), the padded bucket sizes from S and their scan (qAs),
+    // then every kept posting to its place
+    uint32_t *keep = nullptr, *stmp = nullptr, *btmp = nullptr;
+    HC_CUDA(ctx, scr.alloc(&keep, (size_t)qtotal + 1));
+    HC_CUDA(ctx, scr.alloc(&stmp, scan_tmp_words((size_t)qtotal + 1)));
+    HC_CUDA(ctx, scr.alloc(&btmp, scan_tmp_words((size_t)nb + 1)));
+    HC_CUDA(ctx, cudaMemsetAsync(keep + qtotal, 0, 4, st));
+    if (qtotal)
+        k_search_keep<<<(unsigned)std::min<uint64_t>((qtotal + 255) / 256, (uint64_t)ctx->sm_count * 64), 256, 0, st>>>(
+            lh.d_qp, lh.d_qion, qtotal, Lm1, half, lh.d_cls, keep);
     HC_CUDA(ctx, cudaGetLastError());
-    HC_CUDA(ctx, scan_exclusive(lh.d_qAs, (size_t)nb + 1, stmp, st));
+    HC_CUDA(ctx, scan_exclusive(keep, (size_t)qtotal + 1, stmp, st));
+    k_search_counts<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 16), 256, 0, st>>>(
+        lh.d_qA, keep, nb, lh.d_qAs);
+    HC_CUDA(ctx, cudaGetLastError());
+    HC_CUDA(ctx, scan_exclusive(lh.d_qAs, (size_t)nb + 1, btmp, st));
     uint32_t total = 0;
     HC_CUDA(ctx, cudaMemcpyAsync(&total, lh.d_qAs + nb, 4, cudaMemcpyDeviceToHost, st));
     HC_CUDA(ctx, cudaStreamSynchronize(st));
     lh.nsearch = total;
     HC_CUDA(ctx, dalloc(&lh.d_qps, (size_t)total + kIaPad));
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_qps, 0xFF, 4 * ((size_t)total + kIaPad), st));
-    k_search_scatter<<<wblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, lh.d_qion, nb, Lm1, half, lh.d_cls, lh.d_qAs,
-                                              lh.d_qps);
+    if (qtotal)
+        k_search_scatter<<<pblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, keep, nb, qtotal, lh.d_qAs, lh.d_qps);
     HC_CUDA(ctx, cudaGetLastError());
     lh.stride = (n + kRowG - 1) / kRowG + 1;
     HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
