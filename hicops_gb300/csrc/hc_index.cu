@@ -653,7 +653,7 @@ __device__ __forceinline__ bool search_kept(uint32_t x, uint32_t ion, uint32_t L
 }
 
 // keep[i] = 1 for a query posting that stays in the search postings, else 0
-__global__ void k_search_keep(const uint32_t *__restrict__ qp, const uint16_t *__restrict__ qion, uint32_t total,
+__global__ void k_spost_keep(const uint32_t *__restrict__ qp, const uint16_t *__restrict__ qion, uint32_t total,
                               uint32_t Lm1, uint32_t half, const uint8_t *__restrict__ cls, uint32_t *__restrict__ keep)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
@@ -662,7 +662,7 @@ __global__ void k_search_keep(const uint32_t *__restrict__ qp, const uint16_t *_
 
 // the padded size of each bucket's search postings, from the exclusive scan S
 // of the keep flags; entry nb is 0 (the scan makes it the total)
-__global__ void k_search_counts(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ S, uint32_t nb,
+__global__ void k_spost_counts(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ S, uint32_t nb,
                                 uint32_t *__restrict__ qAs)
 {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += gridDim.x * blockDim.x)
@@ -671,7 +671,7 @@ __global__ void k_search_counts(const uint32_t *__restrict__ qA, const uint32_t 
 
 // kPosChunk postings per thread: each kept posting to its place, bucket b's
 // at qAs[b] in their order.
-__global__ void k_search_scatter(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
+__global__ void k_spost_scatter(const uint32_t *__restrict__ qA, const uint32_t *__restrict__ qp,
                                  const uint32_t *__restrict__ S, uint32_t nb, uint32_t total,
                                  const uint32_t *__restrict__ qAs, uint32_t *__restrict__ qps)
 {
@@ -1015,11 +1015,11 @@ int build_rows(hc_ctx *ctx, LenHost &lh)
     HC_CUDA(ctx, scr.alloc(&btmp, scan_tmp_words((size_t)nb + 1)));
     HC_CUDA(ctx, cudaMemsetAsync(keep + qtotal, 0, 4, st));
     if (qtotal)
-        k_search_keep<<<(unsigned)std::min<uint64_t>((qtotal + 255) / 256, (uint64_t)ctx->sm_count * 64), 256, 0, st>>>(
+        k_spost_keep<<<(unsigned)std::min<uint64_t>((qtotal + 255) / 256, (uint64_t)ctx->sm_count * 64), 256, 0, st>>>(
             lh.d_qp, lh.d_qion, qtotal, Lm1, half, lh.d_cls, keep);
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, scan_exclusive(keep, (size_t)qtotal + 1, stmp, st));
-    k_search_counts<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 16), 256, 0, st>>>(
+    k_spost_counts<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, (uint64_t)ctx->sm_count * 16), 256, 0, st>>>(
         lh.d_qA, keep, nb, lh.d_qAs);
     HC_CUDA(ctx, cudaGetLastError());
     HC_CUDA(ctx, scan_exclusive(lh.d_qAs, (size_t)nb + 1, btmp, st));
@@ -1030,7 +1030,7 @@ int build_rows(hc_ctx *ctx, LenHost &lh)
     HC_CUDA(ctx, dalloc(&lh.d_qps, (size_t)total + kIaPad));
     HC_CUDA(ctx, cudaMemsetAsync(lh.d_qps, 0xFF, 4 * ((size_t)total + kIaPad), st));
     if (qtotal)
-        k_search_scatter<<<pblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, keep, nb, qtotal, lh.d_qAs, lh.d_qps);
+        k_spost_scatter<<<pblocks, 256, 0, st>>>(lh.d_qA, lh.d_qp, keep, nb, qtotal, lh.d_qAs, lh.d_qps);
     HC_CUDA(ctx, cudaGetLastError());
     lh.stride = (n + kRowG - 1) / kRowG + 1;
     HC_CUDA(ctx, dalloc(&lh.d_rows, (size_t)nb * lh.stride));
