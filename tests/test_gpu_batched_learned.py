@@ -72,6 +72,44 @@ def test_schedules_graph_and_tuner_agree():
     ix.close()
 
 
+def test_mixed_windows_persistent_edge_cases():
+    """The persistent longest-first schedule on one batch that mixes +-10 ppm,
+    +-5 Da and +-500 Da windows, with variable mods and N-terminal acetylation,
+    a spectrum without valid peaks, intensities that overflow the packed
+    scorecard, and a +-1e-5 Da spectrum whose peaks repeat keys: all equal the
+    oracle."""
+    import torch
+    from hicops_gb300 import dslim
+    from oracle import oracle as O
+    p = S.SearchParams(maxz=3, dF=1, dM=500.0, threads=8, vmods_per_pep=3,
+                       mods=[("M", 15.99, 2), S.NTERM_ACETYL])
+    db = S.make_database(12000, 1301, p)
+    q = S.make_queries(db, 700, 1302, p, peaks=(20, 150),
+                       window_mix=[(0.5, "ppm", 10.0), (0.2, "da", 5.0), (0.3, "da", 500.0)])
+    # spectrum 0: no valid peaks; spectrum 1: every peak twice (keys shared by two peaks);
+    # spectrum 2: intensities >= 2^17
+    idx, moz, inten = q.idx.astype(np.int64), q.moz.copy(), q.intensity.copy()
+    moz[idx[0]:idx[1]] = 0
+    a, b = idx[1], idx[2]
+    half = (b - a) // 2
+    moz[a + half:a + 2 * half] = moz[a:a + half]
+    inten[idx[2]:idx[3]] = inten[idx[2]:idx[3]] + (1 << 17)
+    q = S.QueryBatch(idx=q.idx, moz=moz, intensity=inten, precurse=q.precurse, charges=q.charges,
+                     rtimes=q.rtimes, dM=q.dM)
+    q.dM[1] = 1e-5  # a narrow window for the repeated-key spectrum
+    ores, ohist = O.OracleIndex(db, p).query(q, tie_rule=1)
+    ix = dslim.Index(p)
+    ix.construct_all(db)
+    d, args = _dev(q)
+    ix.set_tuning(schedule=2)
+    ix.query_device(*args)
+    torch.cuda.synchronize()
+    r, h = _results(d, q.nspec)
+    compare(r, h, ores, ohist)
+    assert (ores["cpsms"][q.dM < 1.0] > 0).any() and (ores["cpsms"][q.dM > 100.0] > 0).any()
+    ix.close()
+
+
 def _np_forward_backward(P, X, Y):
     """float64 restatement of the MLP loss and its gradients (the CPU oracle);
     NaN targets add no loss."""
