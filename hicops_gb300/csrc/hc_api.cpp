@@ -144,7 +144,7 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     ctx->lens.resize(nlen);
     for (uint32_t i = 0; i < nlen; i++) ctx->lens[i].L = p->min_len + i;
     // default launch shape: one 1024-thread CTA per SM, 2 postings chunks in
-    // flight per lane, the largest scorecard tile the shared memory holds
+    // flight per lane, the largest scorecard tile that leaves the SM 60 KB of L1
     ctx->tuning.threads = 1024;
     ctx->tuning.tile = max_tile(ctx, p->dF, 1024);
     ctx->tuning.ctas_per_sm = 1;

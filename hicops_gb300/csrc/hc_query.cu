@@ -40,12 +40,20 @@ namespace {
 
 constexpr int kDefer = HC_DEFER_MAX;  // undecided candidates per spectrum, resolved at its end
 constexpr uint32_t kWQ = 128;        // per-warp ring of qualifying candidates (power of two, >= 32 + 64)
-constexpr int kPf = 2;              // lists per thread whose next-job row-table words are loaded early
 constexpr uint32_t kNoJob = 0xFFFFFFFFu;
 constexpr float kApproxErr = 1.1e-4f;
 constexpr float kBinMargin = 2.5e-3f;  // on the x10 scale: 10*(1.1e-4) + float product slack
 constexpr float kNear = 3.5e-4f;       // > 2 * kApproxErr: candidates that may be the top
-constexpr uint32_t kScanSlack = 128;   // scorecard slots past the tile (see smem_layout)
+static_assert(HC_DEFER_MAX >= 128, "the scan's last step may read 127 packed words past the tile, into the queue");
+
+// What the tile loop reads of a length's record: kept in the kernel's
+// parameters (the constant cache; the length index is warp-uniform)
+struct LenS
+{
+    const uint32_t *qp, *rows;  // search postings and their row table
+    uint32_t stride, n;
+    const uint8_t *cls;         // entry classes (4 bytes of padding past the last entry)
+};
 
 struct SearchArgs
 {
@@ -70,6 +78,7 @@ struct SearchArgs
     uint32_t maxz;
     const ClassKeys *classes;   // entry classes (null: none built)
     unsigned long long *phase;  // optional: SM cycles per phase, summed over CTAs (kPhases)
+    LenS len[HC_MAX_LENGTHS];
 };
 
 // phases of k_search timed when SearchArgs::phase is set
@@ -115,22 +124,36 @@ struct Card<true>
     static constexpr int kWords = 2;
 };
 
-// What the tile loop reads of a length's record, kept in shared memory for
-// the kernel's lifetime (one global read per CTA instead of one per job).
-struct LenS
-{
-    const uint32_t *qp, *rows;  // search postings and their row table
-    uint32_t stride, n;
-    const uint8_t *cls;         // entry classes (4 bytes of padding past the last entry)
-};
-
-constexpr uint32_t kMaxDF = 16;  // the largest dF hc_ctx_create accepts
-constexpr uint32_t kMaxGroups = (HC_QALEN * (2 * kMaxDF + 1) + 31) / 32;  // groups of 32 lists
+// histogram bins kept in shared memory; candidates of the bins past them
+// (hyperscores of 25.6 and more: a few per spectrum) add to the spectrum's
+// output histogram directly
+constexpr int kHistSm = 256;
+// float log-factorials kept in shared memory: a packed count stays below 128
+// (a spectrum whose count reaches 128 is redone with wide words)
+constexpr int kLgSm = 128;
 
 struct SmemTail
 {
-    uint32_t hist[HC_HIST_BINS];
-    uint32_t pad0[2];
+    union
+    {
+        // while the spectrum's candidates are scored; lgf first: an
+        // overflowing packed count (up to 255, redone wide) reads histogram
+        // words, inside the block's memory
+        struct
+        {
+            float lgf[kLgSm];
+            uint32_t hist[kHistSm];
+        } run;
+        // during the spectrum's set-up: per entry class, what its y1 keys
+        // collect from the valid peaks as a wide word [count:24 | sum:40]
+        // (kept apart for wide words, whose scorecard start reads it); the
+        // valid peaks that can reach a class key
+        struct
+        {
+            unsigned long long ucls[kMaxClasses + 1];
+            uint32_t low[HC_QALEN];
+        } setup;
+    } u;
     unsigned long long best;   // (exact h bits << 32) | ~(ixx << 24 | psid)
     uint32_t best_shp;
     uint32_t maxbits;          // running max of the float estimate
@@ -143,24 +166,17 @@ struct SmemTail
     uint32_t noret;            // the stream's atomics need not return the old words (see k_search)
     uint32_t pnext;            // next 16-byte chunk (of the tile's lists laid end to end) to hand out
     uint32_t ndefer;           // undecided candidates queued for the exact evaluation
-    uint32_t cchunks[2];       // 16-byte chunks (all lists) of the job in each bound buffer
-    uint32_t ncl[2];           // its non-empty lists
+    uint32_t cchunks;          // 16-byte chunks (all lists) of the job
+    uint32_t ncl;              // its non-empty lists
     unsigned long long bytes;
     unsigned long long ph[kPhases];
     unsigned long long ph_last;
     unsigned long long cnt[4];  // tiles | tiles scanned whole | listed candidates | exact evaluations
     int2 win[HC_MAX_LENGTHS];  // the spectrum's window per length
-    float lgf[kLgTable];
     uint32_t wtail[32];        // per warp: candidates appended to its ring so far (this job)
-    uint32_t gtc[kMaxGroups];  // per group of 32 lists of the next job: chunks
-    uint32_t gtz[kMaxGroups];  // ... and non-empty lists
-    LenS len[HC_MAX_LENGTHS];
     // per entry class: what its y1 keys collect from the spectrum's valid
-    // peaks, as a wide word [count:24 | sum:40] and packed [count:8 |
-    // sum:24]; entry kClassNone stays zero
-    unsigned long long ucls[kMaxClasses + 1];
+    // peaks, packed [count:8 | sum:24]; entry kClassNone stays zero
     uint32_t upk[kMaxClasses + 1];
-    uint32_t low[HC_QALEN];    // valid peaks that can reach a class key
     uint32_t nlow;
 };
 
@@ -177,32 +193,41 @@ struct SmemTail
 
 struct SmemLayout
 {
-    size_t qual, defer, linfo, lend, loff, coff, clid, pmoz, pint, wq, sink, tail, total;
-    uint32_t maxpairs, loffs, clids;  // linfo / loff / coff / clid entries per buffer (two buffers each)
+    size_t qual, defer, lnext, lend, loff, coff, kinfo, pmoz, pint, wq, ucls, sink, tail, total;
+    uint32_t maxpairs;  // lists: valid peaks x bins
 };
 
 __host__ __device__ inline SmemLayout smem_layout(uint32_t tile, uint32_t dF, bool wide, uint32_t nwarps)
 {
     const size_t maxpairs = (size_t)HC_QALEN * (2 * dF + 1);
     SmemLayout o;
-    // packed words: kScanSlack zero slots past the tile, so the scan reads
-    // and clears whole 128-candidate steps without bounds checks
-    o.qual = wide ? (size_t)tile * 16 : ((size_t)tile + kScanSlack) * 8;
+    // the scorecard, then the undecided queue: the scan reads whole
+    // 128-candidate steps, and a window's last step may read up to 127 words
+    // past the tile's end (masked), inside the queue
+    o.qual = wide ? (size_t)tile * 16 : (size_t)tile * 8;
     o.defer = o.qual;
     o.maxpairs = (uint32_t)maxpairs;
-    o.loffs = (uint32_t)maxpairs + 4;
-    o.clids = (uint32_t)maxpairs + 8;
-    o.linfo = o.defer + 8ull * kDefer;         // 16-byte aligned: every size above is a multiple of 16
-    o.lend = o.linfo + 2 * 8 * maxpairs;  // (maxpairs = 100 (2 dF + 1): every size stays a multiple of 16)
+    // per list (of the next job: written while the job streams): its first
+    // posting, the end of its list, its chunk count; per non-empty list of
+    // the job: its first chunk and {first posting, intensity} (the next
+    // job's written after the job's stream)
+    o.lnext = o.defer + 8ull * kDefer;
+    o.lend = o.lnext + 4 * maxpairs;
     o.loff = o.lend + 4 * maxpairs;
-    o.coff = o.loff + 2 * 4 * (maxpairs + 4);
-    o.clid = o.coff + 2 * 4 * (maxpairs + 4);
-    o.pmoz = o.clid + 2 * 2 * (maxpairs + 8);
+    o.coff = o.loff + 4 * (maxpairs + 4);
+    o.kinfo = (o.coff + 4 * (maxpairs + 4) + 7) & ~(size_t)7;
+    o.pmoz = (o.kinfo + 8 * maxpairs + 15) & ~(size_t)15;
     o.pint = o.pmoz + 4ull * HC_QALEN;
     o.wq = (o.pint + 4ull * HC_QALEN + 15) & ~(size_t)15;
-    o.sink = (o.wq + 2ull * kWQ * nwarps + 15) & ~(size_t)15;
+    size_t end = o.wq + 2ull * kWQ * nwarps;
+    // wide words: the class adds, read by every job's scorecard start
+    o.ucls = (end + 15) & ~(size_t)15;
+    if (wide) end = o.ucls + 8ull * (kMaxClasses + 1);
+    o.sink = (end + 15) & ~(size_t)15;
     o.tail = o.sink + 4 * 32;
-    o.total = o.tail + sizeof(SmemTail);
+    // right after the tail: per group of 32 lists of the next job, its chunks
+    // and non-empty lists
+    o.total = o.tail + sizeof(SmemTail) + 8 * ((maxpairs + 31) / 32);
     return o;
 }
 
@@ -308,30 +333,29 @@ __device__ __forceinline__ uint32_t row_hi(const uint32_t *__restrict__ col, uin
 // Step 1, by the warp that computed the group's chunk counts (cnt = this
 // lane's list, 0 past the last list): the group's totals of chunks and of
 // non-empty lists.
-__device__ __forceinline__ void group_totals(uint32_t cnt, uint32_t g, int lane, uint32_t *gtc, uint32_t *gtz)
+__device__ __forceinline__ void group_totals(uint32_t cnt, uint32_t g, int lane, uint2 *gt)
 {
     const uint32_t c = __reduce_add_sync(0xFFFFFFFFu, cnt);
     const uint32_t z = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, cnt != 0u));
-    if (lane == 0)
-    {
-        gtc[g] = c;
-        gtz[g] = z;
-    }
+    if (lane == 0) gt[g] = make_uint2(c, z);
 }
 
 // Step 2, one warp per group, any warp: from the chunk counts lo[0, np) and
-// the group totals, the job's non-empty lists in order: clid[k] = the list,
-// coff[k] = its first chunk (of all lists laid end to end); the warp of the
-// last group (of ng) writes coff[ncl] = *total and the counts.
+// the group totals, the job's non-empty lists in order: coff[k] = its first
+// chunk (of all lists laid end to end), kinfo[k] = {its first posting, its
+// peak's intensity} (list pr = peak pr / nbin, bin pr % nbin); the warp of
+// the last group (of ng) writes coff[ncl] = *total and the counts.
 __device__ __forceinline__ void group_offsets(uint32_t g, uint32_t ng, const uint32_t *lo, uint32_t np, int lane,
-                                              const uint32_t *gtc, const uint32_t *gtz, uint32_t *coff,
-                                              uint16_t *clid, uint32_t *total, uint32_t *ncl)
+                                              const uint2 *gt, const uint32_t *first, const uint32_t *pint,
+                                              uint32_t nbin, uint32_t *coff, uint2 *kinfo, uint32_t *total,
+                                              uint32_t *ncl)
 {
     uint32_t pc = 0, pz = 0;
     for (uint32_t i = (uint32_t)lane; i < g; i += 32)
     {
-        pc += gtc[i];
-        pz += gtz[i];
+        const uint2 t = gt[i];
+        pc += t.x;
+        pz += t.y;
     }
     pc = __reduce_add_sync(0xFFFFFFFFu, pc);
     pz = __reduce_add_sync(0xFFFFFFFFu, pz);
@@ -349,7 +373,7 @@ __device__ __forceinline__ void group_offsets(uint32_t g, uint32_t ng, const uin
     {
         const uint32_t k = pz + (uint32_t)__popc(bal & ((1u << lane) - 1u));
         coff[k] = pc + c - cnt;
-        clid[k] = (uint16_t)pr;
+        kinfo[k] = make_uint2(first[pr], pint[pr / nbin]);
     }
     if (g + 1 == ng && lane == 31)
     {
@@ -425,20 +449,27 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
 {
     using W = typename Card<WIDE>::word;
     constexpr int NW = Card<WIDE>::kWords;
+    // lists per thread whose bucket is kept and whose next-job row-table
+    // words are loaded early (two for blocks of up to 512 threads, one for
+    // 1024: 300 lists at dF = 1 either way; the rest are computed directly)
+    constexpr int kPf = G >= 4 ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t tile = a.tile;
     const uint32_t nbin = 2 * a.dF + 1;
     const SmemLayout L = smem_layout(tile, a.dF, WIDE, blockDim.x >> 5);
     W *card = reinterpret_cast<W *>(smem);
-    uint32_t *coff = reinterpret_cast<uint32_t *>(smem + L.coff);    // per buffer: first chunk of each non-empty list
-    uint16_t *clid = reinterpret_cast<uint16_t *>(smem + L.clid);    // per buffer: which list it is
+    uint32_t *coff = reinterpret_cast<uint32_t *>(smem + L.coff);    // first chunk of each non-empty list
+    uint2 *kinfo = reinterpret_cast<uint2 *>(smem + L.kinfo);         // {first posting, intensity} of each
     uint2 *defer = reinterpret_cast<uint2 *>(smem + L.defer);  // undecided candidates: {b word, y word}
-    uint2 *linfo = reinterpret_cast<uint2 *>(smem + L.linfo);  // per list, two buffers: {first, intensity}
+    uint32_t *lnext = reinterpret_cast<uint32_t *>(smem + L.lnext);  // per list: first posting (next job)
     uint32_t *lend = reinterpret_cast<uint32_t *>(smem + L.lend);  // per list: end of the current job's list
     uint32_t *loff = reinterpret_cast<uint32_t *>(smem + L.loff);
     uint32_t *pmoz = reinterpret_cast<uint32_t *>(smem + L.pmoz);
     uint32_t *pint = reinterpret_cast<uint32_t *>(smem + L.pint);
     SmemTail &T = *reinterpret_cast<SmemTail *>(smem + L.tail);
+    uint2 *gt = reinterpret_cast<uint2 *>(&T + 1);
+    unsigned long long *ucls = WIDE ? reinterpret_cast<unsigned long long *>(smem + L.ucls) : T.u.setup.ucls;
+    uint32_t *low = T.u.setup.low;
 
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, wid = tid >> 5;
@@ -448,13 +479,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     const uint32_t sink_s = (uint32_t)__cvta_generic_to_shared(smem + L.sink) + 4u * (uint32_t)lane;
     uint16_t *wq = reinterpret_cast<uint16_t *>(smem + L.wq) + wid * kWQ;  // this warp's candidate ring (tile < 2^16)
 
-    for (int i = tid; i < kLgTable; i += nthr) T.lgf[i] = a.qc->lgfact_f[i];
-    for (uint32_t l = tid; l < a.nlen; l += nthr)
-    {
-        const LenDev &ld = a.lens[l];
-        T.len[l] = LenS{ld.qps, ld.rows, ld.stride, ld.n, ld.cls};
-    }
-    for (uint32_t i = tid; i < (tile + (WIDE ? 0u : kScanSlack)) * NW; i += nthr) card[i] = 0;
+    for (uint32_t i = tid; i < tile * NW; i += nthr) card[i] = 0;
     if (tid == 0)
     {
         for (int k = 0; k < kPhases; k++) T.ph[k] = 0;
@@ -471,11 +496,15 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
     // hit's estimate is within 2*kApproxErr < kNear of the final maximum, so it
     // is always among them, whatever the order candidates are scored in.
     uint32_t my_cps = 0, my_fl = 0, my_exact = 0;
+    auto hist_add = [&](int bin) {
+        if (bin < kHistSm) atomicAdd(&T.u.run.hist[bin], 1u);
+        else atomicAdd(&a.hist[(size_t)T.spec * HC_HIST_BINS + (uint32_t)bin], 1u);
+    };
     unsigned long long my_best = 0;
     uint32_t my_shp = 0;
     auto score_one = [&](uint32_t bc, uint32_t yc, uint64_t ib, uint64_t iy, uint32_t shp, uint32_t key_lo) {
         float ha;
-        if constexpr (!WIDE) ha = approx_h(T.lgf, bc, yc, ib, iy);
+        if constexpr (!WIDE) ha = approx_h(T.u.run.lgf, bc, yc, ib, iy);
         else ha = exact_h(a.qc, bc, yc, ib, iy);
         const float runmax = __uint_as_float(*(volatile uint32_t *)&T.maxbits);
         if (ha >= runmax - kNear)
@@ -529,7 +558,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         my_cps++;
         if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) my_fl |= HC_FLAG_LGFACT_OOB;
         if (bin >= HC_HIST_BINS || bin < 0) { my_fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
-        atomicAdd(&T.hist[bin], 1u);
+        hist_add(bin);
     };
 
     for (uint32_t iter = 0;; iter++)
@@ -543,10 +572,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             else if (w < a.nspec) sp = a.order ? a.order[w] : w;
             T.spec = sp;
         }
-        for (int i = tid; i < HC_HIST_BINS; i += nthr) T.hist[i] = 0;
         __syncthreads();
         const uint32_t s = T.spec;
         if (s == 0xFFFFFFFFu) break;
+        for (int i = kHistSm + tid; i < HC_HIST_BINS; i += nthr) a.hist[(size_t)s * HC_HIST_BINS + i] = 0;
         if (tid == 0)
         {
             T.best = 0;
@@ -562,7 +591,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             T.nlow = 0;
         }
         for (uint32_t l = tid; l < a.nlen; l += nthr) T.win[l] = a.win[(size_t)s * a.nlen + l];
-        for (uint32_t i = tid; i < kMaxClasses + 1; i += nthr) T.ucls[i] = 0ull;
+        for (uint32_t i = tid; i < kMaxClasses + 1; i += nthr) ucls[i] = 0ull;
         __syncthreads();
         // valid peaks (dslim_query.cpp:625): dF < qion < max*scale - 1 - dF
         {
@@ -580,7 +609,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         pmoz[slot] = q;
                         pint[slot] = a.inten[k];
-                        if (q <= lowlim) T.low[atomicAdd(&T.nlow, 1u)] = slot;
+                        if (q <= lowlim) low[atomicAdd(&T.nlow, 1u)] = slot;
                     }
                 }
             }
@@ -621,21 +650,25 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 unsigned long long acc = 0;
                 for (uint32_t t = 0; t < nlow; t++)
                 {
-                    const uint32_t sl = T.low[t], q = pmoz[sl];
+                    const uint32_t sl = low[t], q = pmoz[sl];
                     if (q <= key + a.dF && q + a.dF >= key) acc += (1ull << 40) | pint[sl];
                 }
-                if (acc) atomicAdd(&T.ucls[c], acc);
+                if (acc) atomicAdd(&ucls[c], acc);
             }
         }
         __syncthreads();
         for (uint32_t i = tid; i < kMaxClasses + 1; i += nthr)
         {
             // packed: a count of 64 or more from a class alone is redone wide
-            const unsigned long long u = T.ucls[i];
+            const unsigned long long u = ucls[i];
             if (!WIDE && (u >> 40) >= 64u) T.overflow = 1;
             T.upk[i] = ((uint32_t)(u >> 40) << 24) | (uint32_t)(u & 0xFFFFFFull);
         }
         __syncthreads();
+        // the set-up's tables are read: their space takes the scoring's (seen
+        // by the scan after the first job's barriers)
+        for (int i = tid; i < kLgSm; i += nthr) T.u.run.lgf[i] = a.qc->lgfact_f[i];
+        for (int i = tid; i < kHistSm; i += nthr) T.u.run.hist[i] = 0;
         const uint32_t np = nv * nbin;
         my_best = 0;
         my_shp = 0;
@@ -646,26 +679,28 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // The spectrum's work is a sequence of jobs (length l, scorecard tile
         // t). Interior tile boundaries are row-table entries; a window's own
         // ends are widened to the nearest ones (see row_lo / row_hi). The
-        // per-list bounds are double-buffered:
-        // while job j streams, the row-table words of job j+1's boundaries are
-        // in flight; right after the stream each thread turns them into job
-        // j+1's bounds. (Asking L2 for job j+1's postings at that point was
-        // measured: it cost more issue slots than the latency it hid.)
+        // per-list bounds are pipelined: while job j streams, the row-table
+        // words of job j+1's boundaries are in flight; right after its own
+        // stream each thread turns them into job j+1's bounds (lnext, lend,
+        // loff), and after the barrier that ends the stream the warps turn
+        // those into job j+1's chunk offsets and {first posting, intensity}
+        // per non-empty list, which only job j+1's stream reads. (Asking L2
+        // for job j+1's postings at that point was measured: it cost more
+        // issue slots than the latency it hid.)
         Job jb = first_job(T.win, a.nlen, tile);
         uint32_t pf_hi[kPf], ps_lo[kPf];
         // the bucket and the intensity of this thread's lists tid + m * nthr
         // (list = (valid peak, bin)): the same for every job of the spectrum
-        uint32_t my_bkt[kPf], my_int[kPf];
+        uint32_t my_bkt[kPf];
 #pragma unroll
         for (int m = 0; m < kPf; m++)
         {
             const uint32_t pr = tid + m * nthr;
-            my_bkt[m] = my_int[m] = 0u;
+            my_bkt[m] = 0u;
             if (pr < np)
             {
                 const uint32_t k = pr / nbin, j = pr - k * nbin;
                 my_bkt[m] = pmoz[k] - a.dF + j;
-                my_int[m] = pint[k];
             }
         }
         uint32_t npass = 0;  // postings of entries inside the window (the reference visits exactly these)
@@ -674,7 +709,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         if (jb.l != kNoJob)
         {
             // the first job's boundaries, directly
-            const LenS d = T.len[jb.l];
+            const LenS d = a.len[jb.l];
             const bool inter = !WIDE && job_interior(jb, d.n);
             for (uint32_t base = 0; base < np; base += (uint32_t)nthr)
             {
@@ -686,12 +721,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t *col = d.rows + (size_t)(pmoz[k] - a.dF + j) * d.stride;
                     const uint32_t st = row_lo(col, jb.c0), en = row_hi(col, jb.c1);
                     if (inter && st < en) npass += en - st;
-                    linfo[pr] = make_uint2(st, pint[k]);
+                    lnext[pr] = st;
                     lend[pr] = en;
                     cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
                     loff[pr] = cnt;
                 }
-                if (base + 32 * (uint32_t)wid < np) group_totals(cnt, (pr >> 5), lane, T.gtc, T.gtz);
+                if (base + 32 * (uint32_t)wid < np) group_totals(cnt, (pr >> 5), lane, gt);
             }
             // the first job's scorecard: each candidate's y word starts with its class's adds
             {
@@ -708,7 +743,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                     else
                     {
-                        const W wy = T.ucls[k];
+                        const W wy = ucls[k];
                         card[2 * c + 1] = wy;
                         npass += (uint32_t)(wy >> 40);
                     }
@@ -716,20 +751,17 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
             __syncthreads();
             for (uint32_t g = nw - 1 - (uint32_t)wid; g < ng; g += nw)
-                group_offsets(g, ng, loff, np, lane, T.gtc, T.gtz, coff, clid, &T.cchunks[0], &T.ncl[0]);
-            if (ng == 0 && tid == 0) T.cchunks[0] = T.ncl[0] = coff[0] = 0;
+                group_offsets(g, ng, loff, np, lane, gt, lnext, pint, nbin, coff, kinfo, &T.cchunks, &T.ncl);
+            if (ng == 0 && tid == 0) T.cchunks = T.ncl = coff[0] = 0;
         }
         __syncthreads();
         while (jb.l != kNoJob)
         {
-            const LenS d = T.len[jb.l];
+            const LenS d = a.len[jb.l];
             const uint32_t c0 = jb.c0, ntile = jb.c1 - jb.c0;
-            uint2 *li_c = linfo + cur * L.maxpairs, *li_n = linfo + (cur ^ 1) * L.maxpairs;
-            uint32_t *lo_n = loff + (cur ^ 1) * L.loffs;  // the next job's chunk counts
-            const uint32_t C = T.cchunks[cur];
-            const uint32_t ncl = T.ncl[cur];
-            const uint32_t *co = coff + cur * L.loffs;
-            const uint16_t *cl = clid + cur * L.clids;
+            const uint32_t C = T.cchunks;
+            const uint32_t ncl = T.ncl;
+            const uint32_t *co = coff;
             HC_PHASE(0);
             // ---- row-table words of the next job's boundaries, in flight ----
             const Job nj = next_job(jb, T.win, a.nlen, tile);
@@ -737,7 +769,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             LenS dn;
             if (nj.l != kNoJob)
             {
-                dn = same ? d : T.len[nj.l];
+                dn = same ? d : a.len[nj.l];
 #pragma unroll
                 for (int m = 0; m < kPf; m++)
                 {
@@ -782,12 +814,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 uint32_t k0 = find_list(co, ncl, q0, lane);
                 if (co[k0 + 1u] >= q0 + 32u * G)  // warp-uniform: the whole grab lies in list k0
                 {
-                    const uint2 li = li_c[cl[k0]];
-                    const uint32_t p0 = (li.x & ~3u) + 4u * (q0 + (uint32_t)lane - co[k0]);
+                    const uint2 ki = kinfo[k0];
+                    const uint32_t p0 = (ki.x & ~3u) + 4u * (q0 + (uint32_t)lane - co[k0]);
+                    const uint32_t li = ki.y;
 #pragma unroll
                     for (int g = 0; g < G; g++)
                     {
-                        inte[g] = li.y;
+                        inte[g] = li;
                         v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + p0 + 128u * g));
                     }
                 }
@@ -803,9 +836,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     {
                         // the group's 32 chunks all lie in list k0 (most
                         // postings sit in long lists): one lookup for the warp
-                        const uint2 li = li_c[cl[k0]];
-                        const uint32_t pos = (li.x & ~3u) + 4u * (kc - co[k0]);
-                        inte[g] = li.y;
+                        const uint2 ki = kinfo[k0];
+                        const uint32_t pos = (ki.x & ~3u) + 4u * (kc - co[k0]);
+                        inte[g] = ki.y;
                         v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
                     }
                     else if (kb < C)  // warp-uniform
@@ -816,13 +849,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         const uint32_t k = k0 + (uint32_t)__popc(msk & ((2u << lane) - 1u));
                         if (kc < C)
                         {
-                            const uint2 li = li_c[cl[k]];
+                            const uint2 ki = kinfo[k];
                             // a chunk never leaves its bucket (buckets start at
                             // multiples of 4, padded to them); its postings
                             // outside [first, end) belong to entries outside
                             // the tile and fail the index test below
-                            const uint32_t pos = (li.x & ~3u) + 4u * (kc - co[k]);
-                            inte[g] = li.y;
+                            const uint32_t pos = (ki.x & ~3u) + 4u * (kc - co[k]);
+                            inte[g] = ki.y;
                             v[g] = __ldg(reinterpret_cast<const uint4 *>(d.qp + pos));
                         }
                         k0 = __shfl_sync(0xFFFFFFFFu, k, 31);  // the list holding chunk kb + 31
@@ -901,12 +934,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         st = same ? lend[pr] : ps_lo[m];
                         en = pf_hi[m];
                         if (inter && st < en) npass += en - st;
-                        li_n[pr] = make_uint2(st, my_int[m]);
+                        lnext[pr] = st;
                         lend[pr] = en;
                         cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                        lo_n[pr] = cnt;
+                        loff[pr] = cnt;
                     }
-                    if (m * nthr + 32 * wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
+                    if (m * nthr + 32 * wid < np) group_totals(cnt, pr >> 5, lane, gt);
                 }
                 // lists past kPf * nthr (small blocks, wide bin windows): directly
                 for (uint32_t base = kPf * nthr; base < np; base += (uint32_t)nthr)
@@ -920,12 +953,12 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                         st = same ? lend[pr] : row_lo(col, nj.c0);
                         en = row_hi(col, nj.c1);
                         if (inter && st < en) npass += en - st;
-                        li_n[pr] = make_uint2(st, pint[k]);
+                        lnext[pr] = st;
                         lend[pr] = en;
                         cnt = st < en ? ((en + 3) >> 2) - (st >> 2) : 0u;
-                        lo_n[pr] = cnt;
+                        loff[pr] = cnt;
                     }
-                    if (base + 32 * (uint32_t)wid < np) group_totals(cnt, pr >> 5, lane, T.gtc, T.gtz);
+                    if (base + 32 * (uint32_t)wid < np) group_totals(cnt, pr >> 5, lane, gt);
                 }
             }
             __syncthreads();
@@ -935,9 +968,8 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             if (nj.l != kNoJob)
             {
                 for (uint32_t g = nw - 1 - (uint32_t)wid; g < ng; g += nw)
-                    group_offsets(g, ng, lo_n, np, lane, T.gtc, T.gtz, coff + (cur ^ 1) * L.loffs,
-                                  clid + (cur ^ 1) * L.clids, &T.cchunks[cur ^ 1], &T.ncl[cur ^ 1]);
-                if (ng == 0 && tid == 0) T.cchunks[cur ^ 1] = T.ncl[cur ^ 1] = coff[(cur ^ 1) * L.loffs] = 0;
+                    group_offsets(g, ng, loff, np, lane, gt, lnext, pint, nbin, coff, kinfo, &T.cchunks, &T.ncl);
+                if (ng == 0 && tid == 0) T.cchunks = T.ncl = coff[0] = 0;
             }
             // ---- every candidate that reached min_shp ----
             // cpsms, histogram and the top hit (see score_one). The packed tile
@@ -970,7 +1002,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 // 31 + 64 entries)
                 auto push = [&](const uint4 w, uint32_t c) {
                     const uint32_t s0 = (w.x >> 24) + (w.y >> 24), s1 = (w.z >> 24) + (w.w >> 24);
-                    const bool q0 = s0 >= a.thr, q1 = s1 >= a.thr;  // thr = max(min_shp, 1)
+                    const bool q0 = s0 >= a.thr && c < ntile, q1 = s1 >= a.thr && c + 1 < ntile;  // thr = max(min_shp, 1)
                     const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, q0), b1 = __ballot_sync(0xFFFFFFFFu, q1);
                     if ((b0 | b1) == 0) return;
                     const uint32_t lt = (1u << lane) - 1u;
@@ -990,8 +1022,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 const bool thr7 = a.thr <= 127u;
                 for (uint32_t base = first; base < ntile; base += step)
                 {
-                    // words past ntile are zero (the tile is cleared after use,
-                    // and the kScanSlack slots past the tile are never written)
+                    // words past ntile are zero up to the tile's end (the clear
+                    // leaves every word past the next job's end zero) and past
+                    // it belong to the queue: a window's last step is masked
                     const uint32_t ca = base + 2 * (uint32_t)lane, cb = ca + 64;
                     const uint4 wa = c4[ca >> 1];
                     const uint4 wb = c4[cb >> 1];
@@ -1009,6 +1042,9 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     const uint32_t sw = bw + yw;
                     uint32_t m = thr7 ? (((sw | 0x80808080u) - thr4) | sw) & 0x80808080u
                                       : (__vcmpgeu4(sw, thr4) & 0x01010101u) << 7;
+                    if (base + 128u > ntile)  // warp-uniform
+                        m &= (ca < ntile ? 0x80u : 0u) | (ca + 1u < ntile ? 0x8000u : 0u) |
+                             (cb < ntile ? 0x800000u : 0u) | (cb + 1u < ntile ? 0x80000000u : 0u);
                     // this lane's place in the warp's ring: from the warp's
                     // append counter (T.wtail = qhead + qh; lanes in any order)
                     const uint32_t n4 = __popc(m);
@@ -1045,7 +1081,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 if (qh) pop_score(qh);
                 // the next job's candidates and their classes (its scorecard start)
                 const uint32_t nn = nj.l != kNoJob ? nj.c1 - nj.c0 : 0u;
-                const uint8_t *ncls = nn ? T.len[nj.l].cls + nj.c0 : nullptr;
+                const uint8_t *ncls = nn ? a.len[nj.l].cls + nj.c0 : nullptr;
                 // the warp's own words, now read: the next job's start there,
                 // four consecutive candidates per lane (b word zero, y word
                 // its class's adds; zero past the next job's end)
@@ -1070,8 +1106,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     }
                     const uint32_t y0 = T.upk[k4 & 0xFFu], y1 = T.upk[(k4 >> 8) & 0xFFu];
                     const uint32_t y2 = T.upk[(k4 >> 16) & 0xFFu], y3 = T.upk[k4 >> 24];
-                    z4[c >> 1] = make_uint4(0u, y0, 0u, y1);
-                    z4[(c >> 1) + 1] = make_uint4(0u, y2, 0u, y3);
+                    if (c < lim)  // words from lim on are zero already (and past the tile not its own)
+                    {
+                        z4[c >> 1] = make_uint4(0u, y0, 0u, y1);
+                        z4[(c >> 1) + 1] = make_uint4(0u, y2, 0u, y3);
+                    }
                     npass += (y0 >> 24) + (y1 >> 24) + (y2 >> 24) + (y3 >> 24);
                 }
             }
@@ -1080,7 +1119,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 // wide words: one candidate per thread, every one checked, then
                 // set to the next job's start (y word: class adds; zero past its end)
                 const uint32_t nn = nj.l != kNoJob ? nj.c1 - nj.c0 : 0u;
-                const uint8_t *ncls = nn ? T.len[nj.l].cls + nj.c0 : nullptr;
+                const uint8_t *ncls = nn ? a.len[nj.l].cls + nj.c0 : nullptr;
                 const uint32_t lim = max(ntile, nn);
                 for (uint32_t c = tid; c < lim; c += nthr)
                 {
@@ -1095,7 +1134,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                     W wy = 0;
                     if (c < nn)
                     {
-                        wy = T.ucls[__ldg(ncls + c)];
+                        wy = ucls[__ldg(ncls + c)];
                         npass += (uint32_t)(wy >> 40);
                     }
                     card[2 * c] = 0;
@@ -1138,7 +1177,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
                 cps++;
                 if (bc >= (uint32_t)kRefMaxShp || yc >= (uint32_t)kRefMaxShp) fl |= HC_FLAG_LGFACT_OOB;
                 if (bin >= HC_HIST_BINS || bin < 0) { fl |= HC_FLAG_HIST_OOB; bin = bin < 0 ? 0 : HC_HIST_BINS - 1; }
-                atomicAdd(&T.hist[bin], 1u);
+                hist_add(bin);
             }
             cps = __reduce_add_sync(0xFFFFFFFFu, cps);
             fl = __reduce_or_sync(0xFFFFFFFFu, fl);
@@ -1166,7 +1205,7 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
             continue;
         }
-        for (int i = tid; i < HC_HIST_BINS; i += nthr) a.hist[(size_t)s * HC_HIST_BINS + i] = T.hist[i];
+        for (int i = tid; i < kHistSm; i += nthr) a.hist[(size_t)s * HC_HIST_BINS + i] = T.u.run.hist[i];
         if (tid == 0)
         {
             hc_result r;
@@ -1523,18 +1562,29 @@ cudaError_t record_stage(hc_ctx *ctx, int i, cudaStream_t st)
                                                : cudaEventRecord(ctx->ev[i], st);
 }
 
+// Shared memory the resident CTAs take at most when a tile is picked, so that
+// the SM keeps 60 KB of its 256 KB as L1 (the next configuration down keeps
+// 28 KB): the search reads its jobs' class codes and row-table words through
+// L1, and with 28 KB it runs 9-10 % slower at the same tile.
+constexpr size_t kSmemKeepL1 = 196 * 1024;
+
 uint32_t max_tile(const hc_ctx *ctx, uint32_t dF, uint32_t threads)
 {
-    return fit_tile(ctx->smem_optin, dF, threads);
+    return max_tile_for(ctx, dF, 1, threads);
 }
 
 uint32_t max_tile_for(const hc_ctx *ctx, uint32_t dF, uint32_t ctas_per_sm, uint32_t threads)
 {
-    if (ctas_per_sm <= 1) return max_tile(ctx, dF, threads);
+    if (ctas_per_sm < 1) ctas_per_sm = 1;
     // the SM's shared memory is split; each CTA also keeps a reserve for the system
-    const size_t per = std::min(ctx->smem_optin, ctx->smem_sm / ctas_per_sm - ctx->smem_reserved);
-    const uint32_t t = fit_tile(per, dF, threads);
-    return smem_layout(t, dF, false, threads / 32).total <= per ? t : 0u;
+    const size_t full = std::min(ctx->smem_optin, ctx->smem_sm / ctas_per_sm - ctx->smem_reserved);
+    const size_t keep = std::min(full, kSmemKeepL1 / ctas_per_sm - ctx->smem_reserved);
+    for (const size_t per : {keep, full})
+    {
+        const uint32_t t = fit_tile(per, dF, threads);
+        if (smem_layout(t, dF, false, threads / 32).total <= per) return t;
+    }
+    return 0u;
 }
 
 int prepare_query(hc_ctx *ctx, uint32_t nspec)
@@ -1602,6 +1652,16 @@ static void fill_lendev(const hc_ctx *ctx, const LenHost &lh, LenDev &d)
     d.cls = lh.d_cls;
 }
 
+// the length records the search kernel keeps in its parameters
+static void fill_lens(const hc_ctx *ctx, SearchArgs &a)
+{
+    for (size_t i = 0; i < ctx->lens.size(); i++)
+    {
+        const LenHost &lh = ctx->lens[i];
+        a.len[i] = LenS{lh.d_qps, lh.d_rows, lh.stride, lh.built ? lh.n : 0u, lh.d_cls};
+    }
+}
+
 int sync_lengths(hc_ctx *ctx)
 {
     if (!ctx->lens_dirty) return HC_SUCCESS;
@@ -1658,6 +1718,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
 
     SearchArgs a{};
     a.lens = ctx->d_lens;
+    fill_lens(ctx, a);
     a.nlen = nlen;
     a.qc = ctx->d_qconst;
     a.idx = d_idx;
@@ -1812,6 +1873,7 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     HC_CUDA(ctx, cudaGetLastError());
     SearchArgs a{};
     a.lens = s.lens;
+    fill_lens(ctx, a);
     a.nlen = nlen;
     a.qc = ctx->d_qconst;
     a.idx = d_idx;
