@@ -11,7 +11,7 @@ Two forms run on the same batch and must give the same PSMs:
   batched+learned  the autotuned persistent kernel (longest windows first,
                    work stealing) replayed from a CUDA graph, then the learned
                    e-value tail (MLP trained here on the plain run's histograms,
-                   expeRT as fallback and judge).
+                   expeRT as fallback and yardstick).
 `value` is the batched+learned spectra/s with the batch resident in HBM; the
 plain form's numbers sit beside it. `e2e` is the host-buffer C-ABI call
 (hc_dslim_query: pinned inputs copied in, results copied out). The index is
@@ -443,7 +443,7 @@ def learned_tail_1m(ix, p, db):
     sub-batches of 100,000 (expeRT e-values); 80 % of the spectra train the network with
     the project's own kernels and the last 20 % are held out: there the learned tail
     decides which spectra it takes (predicted residual within 0.1 and a confirmed
-    first bin) and their e-values are compared with expeRT's (the judge)."""
+    first bin) and their e-values are compared with expeRT's (the yardstick)."""
     import torch
     from hicops_gb300 import dslim
     from hicops_gb300 import synthetic as S

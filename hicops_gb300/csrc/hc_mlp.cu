@@ -1,7 +1,7 @@
 // Learned e-value tail: a 256 -> 128 -> 64 -> 4 MLP (FP32) that maps a
 // spectrum's hyperscore histogram to the tail of its survival function, in
 // place of the per-spectrum regression fit of expeRT (expeRT::ModelTailFit,
-// expeRT.cpp:572-718), which stays the fallback and the judge.
+// expeRT.cpp:572-718), which stays the fallback and the yardstick.
 //
 // Outputs: the tail line (slope, intercept), the first bin of the regression
 // window (expeRT picks it by searching the curve for its 22 % point,

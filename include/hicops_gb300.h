@@ -209,7 +209,7 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
             hc_result *d_out, uint32_t *d_hist, hc_tuning *best, float *best_ms);
 /* ---- learned e-value tail (no reference counterpart; replaces the
  * per-spectrum regression of expeRT::ModelTailFit, expeRT.cpp:572-718, which
- * stays the fallback and the judge) ----
+ * stays the fallback and the yardstick) ----
  * A 256 -> 128 -> 64 -> 4 FP32 MLP mapping a spectrum's histogram (as its log
  * survival curve, bins >= 255 folded) to the tail line (slope, intercept),
  * the first bin of the regression window and the line's RMS residual.

@@ -1,8 +1,8 @@
 /*
  * CPU restatement of the HiCOPS DSLIM search path (TEST INFRASTRUCTURE).
  *
- * This is the oracle: the checker the GPU product is compared with, and the
- * CPU baseline that bench.py times. It is never linked into, loaded by, or
+ * This is the oracle the GPU product is compared with, and the CPU baseline
+ * that bench.py times. It is never linked into, loaded by, or
  * called from the product library. Every function restates one reference
  * function with the same arithmetic (types, evaluation order, truncations),
  * cited file:line inside the reference project (source/core/...).

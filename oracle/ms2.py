@@ -1,6 +1,6 @@
 """CPU restatement of the reference MS2 reader and peak picker.
 
-TEST INFRASTRUCTURE ONLY: the checker for the device MS2 path
+TEST INFRASTRUCTURE ONLY: the oracle for the device MS2 path
 (hicops_gb300/csrc/hc_ms2.cu). Pure Python, for files of a few thousand
 spectra.
 

@@ -1,7 +1,8 @@
 """ctypes front end of the CPU restatement in oracle/hc_oracle.c.
 
-TEST INFRASTRUCTURE ONLY. Imported by tests/, by __graft_entry__.smoke() as
-the checker, and by bench.py's CPU-baseline leg; never by the product package.
+TEST INFRASTRUCTURE ONLY. Imported by tests/, by __graft_entry__.smoke() (to
+compare its results with), and by bench.py's CPU-baseline leg; never by the
+product package.
 """
 from __future__ import annotations
 

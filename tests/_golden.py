@@ -9,7 +9,7 @@ from hicops_gb300 import synthetic as S
 from oracle import oracle as O
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("plain", "mods", "narrow", "plain20k")  # plain20k: configs[0] at its full size
+CASES = ("plain", "mods", "narrow", "plain20k")  # plain20k: the plain workload at its full size (20,000 peptides, 2,000 spectra)
 
 
 def crc(a) -> int:

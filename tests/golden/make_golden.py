@@ -36,7 +36,7 @@ def crc(a: np.ndarray) -> int:
     return zlib.crc32(np.ascontiguousarray(a).tobytes()) & 0xFFFFFFFF
 
 
-# configs[0] at its full size (20,000 peptides, 2,000 spectra, dF 0.02 Da, dM 100 Da,
+# the plain workload at its full size (20,000 peptides, 2,000 spectra, dF 0.02 Da, dM 100 Da,
 # fragment charges 1-2): the histograms are stored as one CRC per spectrum
 FULL = {"plain20k": "plain-20k"}
 

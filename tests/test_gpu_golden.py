@@ -5,7 +5,7 @@ reference byte for byte (CRC). Queries: for every reported spectrum, cpsms,
 histogram, the top hyperscore and tail-fit ints equal the reference's; the top
 hit is the reference's candidate, or (on an exact hyperscore tie, where the
 reference's min-heap decides by insertion order) a candidate with the same
-hyperscore. `plain20k` is configs[0] at its full size (20,000 peptides,
+hyperscore. `plain20k` is the plain workload at its full size (20,000 peptides,
 2,000 spectra, dF 0.02 Da, dM 100 Da).
 """
 import numpy as np
