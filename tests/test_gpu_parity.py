@@ -191,13 +191,16 @@ def test_small_tiles(dslim, orc):
 @pytest.mark.parametrize("threads,ppw", [(64, 1), (128, 2)])
 def test_small_blocks(dslim, orc, threads, ppw):
     """Blocks smaller than a third of the (peak, bin) lists: list bounds past
-    the per-thread prefetch slots are computed directly."""
+    the per-thread prefetch slots are computed directly. The batch also has
+    candidates in histogram bins from 256 on (hyperscores of 25.6 and more),
+    which the kernel adds to the output histogram directly."""
     p, db, q = case("mods", 20000, 120, 818)
     ix = dslim.Index(p)
     ix.construct_all(db)
     ix.set_tuning(tile=4096, threads=threads, pairs_per_warp=ppw, ctas_per_sm=1)
     res, hist = ix.query(q)
     ores, ohist = orc.OracleIndex(db, p).query(q, tie_rule=1)
+    assert (ohist.reshape(q.nspec, -1)[:, 256:] > 0).any()
     compare(res, hist, ores, ohist)
     ix.close()
 
