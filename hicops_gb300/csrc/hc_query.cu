@@ -796,9 +796,10 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             constexpr bool NR = decltype(no_return)::value;
             constexpr bool CNT = decltype(count)::value;
             (void)NR;
-            unsigned char *cardb = reinterpret_cast<unsigned char *>(card);
-            const uint32_t base8 = c0 << kQpEntryShift, lim8 = ntile << kQpEntryShift;
-            const uint32_t base2 = 2 * c0, lim2 = 2 * ntile;
+            (void)CNT;
+            // packed: byte offsets of the tile's words; wide: word indexes
+            [[maybe_unused]] const uint32_t base8 = c0 << kQpEntryShift, lim8 = ntile << kQpEntryShift;
+            [[maybe_unused]] const uint32_t base2 = 2 * c0, lim2 = 2 * ntile;
             for (;;)
             {
                 uint32_t q0 = 0;
