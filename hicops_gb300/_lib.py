@@ -49,7 +49,8 @@ class HcParams(C.Structure):
 
 class HcTuning(C.Structure):
     _fields_ = [("threads", C.c_uint32), ("tile", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("pairs_per_warp", C.c_uint32), ("schedule", C.c_uint32), ("defer_cap", C.c_uint32)]
+                ("pairs_per_warp", C.c_uint32), ("schedule", C.c_uint32), ("defer_cap", C.c_uint32),
+                ("small_log2", C.c_uint32)]
 
 
 def to_hc_params(p) -> HcParams:

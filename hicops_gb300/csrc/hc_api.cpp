@@ -151,6 +151,7 @@ int hc_ctx_create(int device, const hc_params *p, hc_ctx **out)
     ctx->tuning.pairs_per_warp = 2;
     ctx->tuning.schedule = 0;
     ctx->tuning.defer_cap = HC_DEFER_MAX;
+    ctx->tuning.small_log2 = 0;
     *out = ctx;
     return HC_SUCCESS;
 }
@@ -193,7 +194,7 @@ int hc_ctx_set_tuning(hc_ctx *ctx, const hc_tuning *t)
         t->tile > 32768 ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 8 ||
         (t->pairs_per_warp != 1 && t->pairs_per_warp != 2 && t->pairs_per_warp != 4 && t->pairs_per_warp != 8) ||
-        t->schedule > 2 || t->defer_cap > HC_DEFER_MAX)
+        t->schedule > 2 || t->defer_cap > HC_DEFER_MAX || t->small_log2 > 40)
         return set_error(ctx, HC_ERR_INVLD_PARAM, "bad tuning");
     const size_t need = search_smem(t->tile, ctx->p.dF, false, t->threads);
     if (t->ctas_per_sm * (need + ctx->smem_reserved) > ctx->smem_sm || need > ctx->smem_optin)

@@ -132,7 +132,7 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
     cudaStream_t st = ctx->stream;
     const hc_tuning saved = ctx->tuning;
     // stage 1: schedule x CTAs per SM x block size x chunks in flight, each with
-    // the largest scorecard tile that fits
+    // the largest scorecard tile that fits (small windows in the same launch)
     std::vector<hc_tuning> cand;
     for (uint32_t sched : {0u, 2u})
         for (uint32_t cps : {1u, 2u})
@@ -197,6 +197,26 @@ int hc_tune(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uin
         {
             run(t);
             if (rc) break;
+        }
+    }
+    // stage 3: the fastest longest-first shape with the small-window spectra
+    // in a launch of their own, for a few split points
+    if (!rc)
+    {
+        const auto best2 = std::min_element(timed.begin(), timed.end(), [](const auto &a, const auto &b) {
+            if ((a.second.schedule == 2) != (b.second.schedule == 2)) return a.second.schedule == 2;
+            return a.first < b.first;
+        });
+        if (best2 != timed.end() && best2->second.schedule == 2)
+        {
+            const hc_tuning base = best2->second;
+            for (uint32_t lg : {12u, 15u, 18u})
+            {
+                hc_tuning t = base;
+                t.small_log2 = lg;
+                run(t);
+                if (rc) break;
+            }
         }
     }
     ctx->profiling = prof;

@@ -155,6 +155,12 @@ struct ScratchPtrs
     LenDev *lens;       // HC_MAX_LENGTHS
 };
 
+// Per-query counters (device words): the searches' work counters, the
+// overflow list's length, the small-window split point of the longest-first
+// order, then its per-class counts and cursors.
+constexpr uint32_t kWkSearch = 0, kWkWide = 1, kWkNwide = 2, kWkSmall = 3, kWkSplit = 4;
+constexpr uint32_t kWkCnt = 8, kWkCur = kWkCnt + 64, kWorkWords = kWkCur + 64;
+
 // What a captured query graph was recorded with; a call that differs re-captures.
 struct GraphKey
 {

@@ -39,7 +39,7 @@ constexpr size_t al(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 constexpr size_t kWinOff = 0;
 constexpr size_t kWideOff = kWinOff + al(sizeof(int2) * (size_t)kNoAllocMaxSpectra * HC_MAX_LENGTHS);
 constexpr size_t kWorkOff = kWideOff + al(4ull * (kNoAllocMaxSpectra + 4));
-constexpr size_t kOrderOff = kWorkOff + al(4ull * (4 + 2 * 64));
+constexpr size_t kOrderOff = kWorkOff + al(4ull * kWorkWords);
 constexpr size_t kFitOff = kOrderOff + al(8ull * kNoAllocMaxSpectra);
 constexpr size_t kLensOff = kFitOff + al(4ull * kNoAllocMaxSpectra);
 constexpr size_t kScratchBytes = kLensOff + al(sizeof(LenDev) * HC_MAX_LENGTHS);  // about 8.5 MB

@@ -74,6 +74,8 @@ struct SearchArgs
     const uint32_t *only;   // optional list of spectra to process (wide pass)
     const uint32_t *nonly_dev;  // its length, in device memory
     const uint32_t *order;  // optional processing order (longest first)
+    const uint32_t *obase;  // optional (device word): the first position of the order this launch takes
+    const uint32_t *olim;   // optional (device word): the position it stops at (else nspec)
     uint32_t persistent;    // 1: CTAs loop over a work counter; 0: one spectrum per CTA
     uint32_t maxz;
     const ClassKeys *classes;   // entry classes (null: none built)
@@ -569,7 +571,11 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             const uint32_t w = a.persistent ? atomicAdd(a.work, 1u) : (iter == 0 ? blockIdx.x : 0xFFFFFFFFu);
             uint32_t sp = 0xFFFFFFFFu;
             if (a.only) sp = w < *a.nonly_dev ? a.only[w] : 0xFFFFFFFFu;
-            else if (w < a.nspec) sp = a.order ? a.order[w] : w;
+            else
+            {
+                const uint32_t o = (a.obase ? *a.obase : 0u) + w;
+                if (w < a.nspec && o < (a.olim ? *a.olim : a.nspec)) sp = a.order ? a.order[o] : o;
+            }
             T.spec = sp;
         }
         __syncthreads();
@@ -1514,8 +1520,12 @@ __global__ void k_cost(const int2 *__restrict__ win, uint32_t nspec, uint32_t nl
     atomicAdd(&cnt[k], 1u);
 }
 
+// split (optional): the number of spectra whose cost class exceeds
+// split_class, i.e. whose windows hold 2^split_class candidates or more in all
+// (they come first in the order)
 __global__ void k_order(const uint32_t *__restrict__ cls, uint32_t nspec, const uint32_t *__restrict__ cnt,
-                        uint32_t *__restrict__ cursor, uint32_t *__restrict__ order)
+                        uint32_t *__restrict__ cursor, uint32_t *__restrict__ order, uint32_t split_class,
+                        uint32_t *__restrict__ split)
 {
     __shared__ uint32_t off[kCostClasses];
     if (threadIdx.x == 0)
@@ -1526,6 +1536,7 @@ __global__ void k_order(const uint32_t *__restrict__ cls, uint32_t nspec, const 
             off[k] = run;
             run += cnt[k];
         }
+        if (split && blockIdx.x == 0) *split = off[split_class];
     }
     __syncthreads();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1598,7 +1609,7 @@ int prepare_query(hc_ctx *ctx, uint32_t nspec)
     if ((rc = grow(ctx, &q.d_wide, &q.wide_cap, (size_t)nspec + 4))) return rc;
     if ((rc = grow(ctx, &q.d_order, &q.order_cap, 2 * (size_t)nspec))) return rc;
     if ((rc = grow(ctx, &q.d_fitstart, &q.fit_cap, (size_t)nspec))) return rc;
-    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * (4 + 2 * 64)));
+    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * kWorkWords));
     return HC_SUCCESS;
 }
 
@@ -1690,6 +1701,48 @@ static int grow(hc_ctx *ctx, T **p, size_t *cap, size_t need)
     return HC_SUCCESS;
 }
 
+// The packed search of a batch: with schedule 2 the longest-first order first,
+// then one launch of the tuned shape or, when small windows have their own
+// launch, two: the tuned shape takes the order up to the split point and
+// 128-thread CTAs, kSmallCtas per SM, the rest (spectra that are mostly
+// fixed per-job latency gain from more of them in flight per SM). Both read
+// their range of the order on the device.
+constexpr uint32_t kSmallThreads = 128, kSmallCtas = 6;
+
+static int launch_packed(hc_ctx *ctx, SearchArgs &a, uint32_t sched, uint32_t nspec, uint32_t nlen, const int2 *win,
+                         uint32_t *order, uint32_t *work, cudaStream_t st, int &launches, bool stages)
+{
+    const hc_tuning &t = ctx->tuning;
+    const uint32_t small_tile = max_tile_for(ctx, a.dF, kSmallCtas, kSmallThreads);
+    const bool split = sched == 2 && t.small_log2 != 0 && small_tile >= kRowG;
+    a.obase = a.olim = nullptr;
+    if (sched == 2)
+    {
+        uint32_t *cls = order + nspec;
+        k_cost<<<(nspec + 255) / 256, 256, 0, st>>>(win, nspec, nlen, cls, work + kWkCnt);
+        k_order<<<(nspec + 255) / 256, 256, 0, st>>>(cls, nspec, work + kWkCnt, work + kWkCur, order,
+                                                     split ? t.small_log2 : 0u, split ? work + kWkSplit : nullptr);
+        HC_CUDA(ctx, cudaGetLastError());
+        a.order = order;
+        launches += 2;
+        if (split) a.olim = work + kWkSplit;
+    }
+    // the search stage: the packed launches
+    if (stages) HC_CUDA(ctx, record_stage(ctx, 1, st));
+    const size_t smem = search_smem(a.tile, a.dF, false, t.threads);
+    const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)t.ctas_per_sm;
+    int rc = launch_search<false>(ctx, a, grid, t.threads, smem, t.pairs_per_warp, st);
+    if (rc || !split) return rc;
+    SearchArgs s = a;
+    s.obase = work + kWkSplit;
+    s.olim = nullptr;
+    s.work = work + kWkSmall;
+    s.tile = small_tile;
+    launches++;
+    return launch_search<false>(ctx, s, ctx->sm_count * (int)kSmallCtas, kSmallThreads,
+                                search_smem(small_tile, s.dF, false, kSmallThreads), 2, st);
+}
+
 int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, const uint32_t *d_int,
                  const float *d_prec, const double *d_dM, uint32_t nspec, uint32_t npeaks,
                  hc_result *d_out, uint32_t *d_hist, cudaStream_t st, bool tailfit)
@@ -1707,9 +1760,9 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     const uint32_t sched = ctx->tuning.schedule;
     if (sched == 2 && (rc = grow(ctx, &q.d_order, &q.order_cap, 2 * (size_t)nspec))) return rc;
     if ((rc = grow(ctx, &q.d_fitstart, &q.fit_cap, (size_t)nspec))) return rc;
-    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * (4 + 2 * 64)));
-    q.d_nwide = q.d_work + 2;
-    HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 4 * (4 + 2 * 64), st));
+    if (!q.d_work) HC_CUDA(ctx, cudaMalloc((void **)&q.d_work, 4 * kWorkWords));
+    q.d_nwide = q.d_work + kWkNwide;
+    HC_CUDA(ctx, cudaMemsetAsync(q.d_work, 0, 4 * kWorkWords, st));
 
     const uint64_t nw = (uint64_t)nspec * nlen;
     if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 0, st));
@@ -1744,19 +1797,7 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     a.classes = ctx->d_classes;
     a.phase = ctx->d_phase;
     int launches = 4;
-    if (sched == 2)
-    {
-        uint32_t *cls = q.d_order + nspec, *cnt = q.d_work + 4, *cur = q.d_work + 4 + 64;
-        k_cost<<<(nspec + 255) / 256, 256, 0, st>>>(q.d_win, nspec, nlen, cls, cnt);
-        k_order<<<(nspec + 255) / 256, 256, 0, st>>>(cls, nspec, cnt, cur, q.d_order);
-        HC_CUDA(ctx, cudaGetLastError());
-        a.order = q.d_order;
-        launches += 2;
-    }
-    const size_t smem = search_smem(a.tile, a.dF, false, ctx->tuning.threads);
-    const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
-    if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 1, st));
-    int rc2 = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
+    int rc2 = launch_packed(ctx, a, sched, nspec, nlen, q.d_win, q.d_order, q.d_work, st, launches, ctx->profiling);
     if (rc2) return rc2;
     if (ctx->profiling) HC_CUDA(ctx, record_stage(ctx, 2, st));
     // spectra whose packed scorecard could overflow are redone wide; the
@@ -1767,7 +1808,8 @@ int query_device(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_moz, cons
     b.order = nullptr;
     b.only = q.d_wide;
     b.nonly_dev = q.d_nwide;
-    b.work = q.d_work + 1;
+    b.work = q.d_work + kWkWide;
+    b.obase = b.olim = nullptr;
     b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
     const size_t smem2 = search_smem(b.tile, b.dF, true, ctx->tuning.threads);
     rc2 = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, smem2, 2, st);
@@ -1867,8 +1909,8 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     HC_CUDA(ctx, cudaGetLastError());
     ctx->last_launches = 0;
     if (nspec == 0) return HC_SUCCESS;
-    uint32_t *nwide = s.work + 2;
-    HC_CUDA(ctx, cudaMemsetAsync(s.work, 0, 4 * (4 + 2 * 64), st));
+    uint32_t *nwide = s.work + kWkNwide;
+    HC_CUDA(ctx, cudaMemsetAsync(s.work, 0, 4 * kWorkWords, st));
     const uint64_t nw = (uint64_t)nspec * nlen;
     k_windows<<<(unsigned)((nw + 255) / 256), 256, 0, st>>>(s.lens, nlen, d_prec, d_dM, ctx->p.dM, nspec, s.win);
     HC_CUDA(ctx, cudaGetLastError());
@@ -1899,25 +1941,15 @@ int launch_query_scratch(hc_ctx *ctx, const uint32_t *d_idx, const uint32_t *d_m
     a.maxz = ctx->p.maxz;
     a.classes = ctx->d_classes;
     int launches = 4;
-    if (sched == 2)
-    {
-        uint32_t *cls = s.order + nspec, *cnt = s.work + 4, *cur = s.work + 4 + 64;
-        k_cost<<<(nspec + 255) / 256, 256, 0, st>>>(s.win, nspec, nlen, cls, cnt);
-        k_order<<<(nspec + 255) / 256, 256, 0, st>>>(cls, nspec, cnt, cur, s.order);
-        HC_CUDA(ctx, cudaGetLastError());
-        a.order = s.order;
-        launches += 2;
-    }
-    const size_t smem = search_smem(a.tile, a.dF, false, ctx->tuning.threads);
-    const int grid = sched == 1 ? (int)nspec : ctx->sm_count * (int)ctx->tuning.ctas_per_sm;
-    int rc = launch_search<false>(ctx, a, grid, ctx->tuning.threads, smem, ctx->tuning.pairs_per_warp, st);
+    int rc = launch_packed(ctx, a, sched, nspec, nlen, s.win, s.order, s.work, st, launches, false);
     if (rc) return rc;
     SearchArgs b = a;
     b.persistent = 1;
     b.order = nullptr;
     b.only = s.wide;
     b.nonly_dev = nwide;
-    b.work = s.work + 1;
+    b.work = s.work + kWkWide;
+    b.obase = b.olim = nullptr;
     b.tile = std::max(kRowG, ctx->tuning.tile / 2 / kRowG * kRowG);  // same shared memory, 16-byte words
     rc = launch_search<true>(ctx, b, ctx->sm_count, ctx->tuning.threads, search_smem(b.tile, b.dF, true, ctx->tuning.threads), 2, st);
     if (rc) return rc;

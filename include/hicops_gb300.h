@@ -122,6 +122,10 @@ typedef struct hc_tuning
                               bin the float estimate leaves open, queued for one exact
                               evaluation at the spectrum's end (<= HC_DEFER_MAX; 0: each
                               is evaluated in place). Results do not depend on it. */
+    uint32_t small_log2;   /* schedule 2: spectra whose windows hold fewer than
+                              2^small_log2 candidates in all run in a second launch of
+                              128-thread CTAs, several per SM, after the others (0: none;
+                              at most 40). Results do not depend on it. */
 } hc_tuning;
 #define HC_DEFER_MAX 128
 

@@ -72,12 +72,15 @@ def test_schedules_graph_and_tuner_agree():
     ix.close()
 
 
-def test_mixed_windows_persistent_edge_cases():
+@pytest.mark.parametrize("small_log2", [0, 15, 40])
+def test_mixed_windows_persistent_edge_cases(small_log2):
     """The persistent longest-first schedule on one batch that mixes +-10 ppm,
     +-5 Da and +-500 Da windows, with variable mods and N-terminal acetylation,
     a spectrum without valid peaks, intensities that overflow the packed
     scorecard, and a +-1e-5 Da spectrum whose peaks repeat keys: all equal the
-    oracle."""
+    oracle. small_log2: the spectra whose windows hold fewer than 2^small_log2
+    candidates run in a second, small-block launch (none; the narrow windows;
+    every spectrum)."""
     import torch
     from hicops_gb300 import dslim
     from oracle import oracle as O
@@ -101,7 +104,7 @@ def test_mixed_windows_persistent_edge_cases():
     ix = dslim.Index(p)
     ix.construct_all(db)
     d, args = _dev(q)
-    ix.set_tuning(schedule=2)
+    ix.set_tuning(schedule=2, small_log2=small_log2)
     ix.query_device(*args)
     torch.cuda.synchronize()
     r, h = _results(d, q.nspec)
