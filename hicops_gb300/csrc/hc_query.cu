@@ -710,7 +710,6 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             }
         }
         uint32_t npass = 0;  // postings of entries inside the window (the reference visits exactly these)
-        uint32_t cur = 0;
         const uint32_t nw = (uint32_t)nthr >> 5, ng = (np + 31) >> 5;
         if (jb.l != kNoJob)
         {
@@ -1163,7 +1162,6 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
             if (tid == 0) T.pnext = 0;
             __syncthreads();
             HC_PHASE(3);
-            cur ^= 1;
             jb = nj;
         }
         // ---- candidates whose sign or bin the float estimate left open ----
