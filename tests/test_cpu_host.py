@@ -25,6 +25,32 @@ def test_library_exports_every_declared_symbol():
     assert lib.hc_version() >= 10000
 
 
+def _header_fields(hdr: str, name: str) -> list:
+    """Field names, in order, of `typedef struct name { ... } name;` in the header."""
+    body = re.search(r"typedef struct %s\s*\{(.*?)\}\s*%s;" % (name, name), hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r"^(const\s+)?[A-Za-z_0-9]+\s+", "", decl)  # the type
+        for v in decl.split(","):
+            names.append(re.match(r"\s*\**\s*([A-Za-z_0-9]+)", v).group(1))
+    return names
+
+
+def test_ctypes_mirrors_match_the_header():
+    """The Python mirrors of the ABI's structs list the header's fields in its
+    order (a drift would pass values into the wrong fields)."""
+    with open(os.path.join(ROOT, "include", "hicops_gb300.h")) as f:
+        hdr = f.read()
+    assert _header_fields(hdr, "hc_tuning") == [n for n, _ in L.HcTuning._fields_]
+    assert _header_fields(hdr, "hc_params") == [n for n, _ in L.HcParams._fields_]
+    assert _header_fields(hdr, "hc_entry") == list(L.ENTRY_DTYPE.names)
+    assert _header_fields(hdr, "hc_result") == list(L.RESULT_DTYPE.names)
+
+
 def test_ctx_create_without_device_fails_loudly():
     import torch
     if torch.cuda.is_available():
