@@ -76,6 +76,7 @@ struct SearchArgs
     const uint32_t *order;  // optional processing order (longest first)
     const uint32_t *obase;  // optional (device word): the first position of the order this launch takes
     const uint32_t *olim;   // optional (device word): the position it stops at (else nspec)
+    uint32_t always_return; // the stream's atomics always return the old words (no all-pairs peak test)
     uint32_t persistent;    // 1: CTAs loop over a work counter; 0: one spectrum per CTA
     uint32_t maxz;
     const ClassKeys *classes;   // entry classes (null: none built)
@@ -627,7 +628,13 @@ __global__ void __launch_bounds__(G >= 4 ? 512 : 1024, G == 4 ? 2 : 1) k_search(
         // its own (valid peaks more than 2*dF bins apart), a candidate's b (y)
         // count is at most its number of b (y) ions, (L-1)*maxz, below 128 for
         // every length; with intensities below 2^17 the sums stay below 2^24.
-        if constexpr (!WIDE)
+        // (The small-window launch skips the all-pairs test: its spectra visit
+        // few postings, so returning atomics cost less than the test.)
+        if (!WIDE && a.always_return)
+        {
+            if (tid == 0) T.noret = 0u;
+        }
+        else if constexpr (!WIDE)
         {
             // warp w takes peaks i = w, w + nw, ...; its lanes the peaks j > i
             bool close = false;
@@ -1736,6 +1743,7 @@ static int launch_packed(hc_ctx *ctx, SearchArgs &a, uint32_t sched, uint32_t ns
     s.olim = nullptr;
     s.work = work + kWkSmall;
     s.tile = small_tile;
+    s.always_return = 1;
     launches++;
     return launch_search<false>(ctx, s, ctx->sm_count * (int)kSmallCtas, kSmallThreads,
                                 search_smem(small_tile, s.dF, false, kSmallThreads), 2, st);
